@@ -1,0 +1,121 @@
+"""ctypes binding of libghcm.so (the C ABI declared in include/ghcm.h)."""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libghcm.so"
+
+GHCM_OK = 0
+GHCM_ERR_BAD_ARG = -1
+GHCM_ERR_BAD_INPUT = -2
+GHCM_ERR_OOM = -3
+GHCM_ERR_CUDA = -4
+GHCM_ERR_TIMEOUT = -5
+GHCM_ERR_NOT_CONVERGED = -6
+GHCM_ERR_UNSUPPORTED = -7
+GHCM_ERR_INTERNAL = -8
+
+GHCM_KERNEL_SYSTOLIC = 0
+GHCM_KERNEL_FIM = 1
+GHCM_SCHEDULE_PLAIN = 0
+GHCM_SCHEDULE_LEARNED = 1
+GHCM_KEY_BOUNDARY_MIN = 0
+GHCM_KEY_BLOCK_MIN = 1
+
+# Every entry point include/ghcm.h declares.
+EXPORTS = (
+    "ghcm_config_default",
+    "ghcm_create",
+    "ghcm_destroy",
+    "ghcm_solve",
+    "ghcm_solve_device",
+    "ghcm_device_sm_count",
+    "ghcm_status_string",
+    "ghcm_abi_version",
+    "ghcm_selftest_wait_timeout",
+)
+
+
+class GhcmConfig(ctypes.Structure):
+    _fields_ = [
+        ("block_size", ctypes.c_uint32),
+        ("max_jobs", ctypes.c_uint32),
+        ("eps", ctypes.c_float),
+        ("kernel", ctypes.c_uint32),
+        ("schedule", ctypes.c_uint32),
+        ("key_mode", ctypes.c_uint32),
+        ("max_sweeps", ctypes.c_uint32),
+        ("max_waves", ctypes.c_uint32),
+        ("wait_timeout_ms", ctypes.c_uint32),
+        ("device", ctypes.c_int32),
+        ("use_tma", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 5),
+    ]
+
+
+class GhcmStats(ctypes.Structure):
+    _fields_ = [
+        ("block_solves", ctypes.c_uint64),
+        ("cells", ctypes.c_uint64),
+        ("bytes_alg", ctypes.c_uint64),
+        ("waves", ctypes.c_uint32),
+        ("residual_passes", ctypes.c_uint32),
+        ("max_active", ctypes.c_uint32),
+        ("tiles", ctypes.c_uint32),
+        ("device_ms", ctypes.c_double),
+        ("total_ms", ctypes.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class GhcmError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: {status_string(status)} ({status})" if what else f"{status_string(status)} ({status})")
+
+
+_lib = None
+
+
+def load(path: Path | None = None):
+    """Loads libghcm.so; raises if it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: build it with `python -m ghcm_gb300.build`")
+    lib = ctypes.CDLL(str(p))
+    f32p = ctypes.POINTER(ctypes.c_float)
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+    cfgp = ctypes.POINTER(GhcmConfig)
+    stp = ctypes.POINTER(GhcmStats)
+    vp = ctypes.c_void_p
+    lib.ghcm_config_default.argtypes = [cfgp]
+    lib.ghcm_create.argtypes = [cfgp, ctypes.POINTER(vp)]
+    lib.ghcm_destroy.argtypes = [vp]
+    lib.ghcm_solve.argtypes = [vp, f32p, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, u32p,
+                               ctypes.c_uint32, f32p, stp]
+    lib.ghcm_solve_device.argtypes = [vp, vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, vp,
+                                      ctypes.c_uint32, vp, vp, stp]
+    lib.ghcm_device_sm_count.argtypes = [vp, u32p]
+    lib.ghcm_status_string.argtypes = [ctypes.c_int]
+    lib.ghcm_status_string.restype = ctypes.c_char_p
+    lib.ghcm_abi_version.argtypes = []
+    lib.ghcm_selftest_wait_timeout.argtypes = [vp, ctypes.c_uint32]
+    for name in EXPORTS:
+        if name != "ghcm_status_string":
+            getattr(lib, name).restype = ctypes.c_int
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def status_string(status: int) -> str:
+    try:
+        return load().ghcm_status_string(int(status)).decode()
+    except FileNotFoundError:
+        return "library not built"

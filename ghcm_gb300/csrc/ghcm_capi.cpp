@@ -1,0 +1,399 @@
+// C-ABI layer of libghcm.so: contexts, device workspace, argument checks,
+// tensor-map setup and the launch sequence of one solve.
+//
+// Replaces the host half of the reference's gHCM path:
+//   eikonal_hcm_opencl_setup (src/eikonal_hcm.cpp:137-175) -> ghcm_create
+//   eikonal_hcm_opencl_ex    (src/eikonal_hcm.cpp:186-529) -> ghcm_solve / ghcm_solve_device
+// The reference's per-wave host loop (priority queue, job upload, blocking
+// status read, neighbour activation) has no host counterpart here: it runs on
+// the device inside one persistent kernel (ghcm_solver.cu).
+#include "../../include/ghcm.h"
+#include "ghcm_internal.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+namespace {
+
+using namespace ghcm;
+
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    bool reserve(size_t need) {
+        if (need <= bytes) return true;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (cudaMalloc(&p, need) != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            return false;
+        }
+        bytes = need;
+        return true;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct ghcm_ctx {
+    ghcm_config cfg;
+    int device = 0;
+    int sms = 0;
+    LaunchInfo launch{};
+    EncodeTiledFn encode = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // scheduler workspace: flags | key | tmin | list0 | list1 | jobs | ctl | insts
+    DevBuf ws;
+    // field buffers used by ghcm_solve (host-pointer entry)
+    DevBuf d_in, d_time, d_seeds;
+    // pinned staging for the instance record and the control block readback
+    Inst* h_inst = nullptr;
+    Ctl* h_ctl = nullptr;
+};
+
+namespace {
+
+int map_cuda(cudaError_t e) {
+    if (e == cudaSuccess) return GHCM_OK;
+    if (e == cudaErrorMemoryAllocation) return GHCM_ERR_OOM;
+    return GHCM_ERR_CUDA;
+}
+
+int check_config(const ghcm_config* c) {
+    if (!c) return GHCM_ERR_BAD_ARG;
+    if (c->block_size != 8 && c->block_size != 16 && c->block_size != 32) return GHCM_ERR_BAD_ARG;
+    if (c->kernel > GHCM_KERNEL_FIM || c->schedule > GHCM_SCHEDULE_LEARNED || c->key_mode > GHCM_KEY_BLOCK_MIN)
+        return GHCM_ERR_BAD_ARG;
+    if (!(c->eps >= 0.f) || !std::isfinite(c->eps)) return GHCM_ERR_BAD_ARG;
+    for (uint32_t r : c->reserved)
+        if (r != 0) return GHCM_ERR_BAD_ARG;
+    return GHCM_OK;
+}
+
+struct Layout {
+    size_t flags, key, tmin, list0, list1, jobs, ctl, insts, total;
+};
+
+Layout layout_for(uint32_t tiles, uint32_t jobs) {
+    Layout l{};
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t const at = o;
+        o = align_up(o + bytes, 256);
+        return at;
+    };
+    l.flags = take(sizeof(uint32_t) * tiles);
+    l.key = take(sizeof(uint32_t) * tiles);
+    l.tmin = take(sizeof(float) * tiles);
+    l.list0 = take(sizeof(uint32_t) * tiles);
+    l.list1 = take(sizeof(uint32_t) * tiles);
+    l.jobs = take(sizeof(uint32_t) * std::max<uint32_t>(jobs, 1));
+    l.ctl = take(sizeof(Ctl));
+    l.insts = take(sizeof(Inst));
+    l.total = o;
+    return l;
+}
+
+bool encode_map(ghcm_ctx* ctx, CUtensorMap* map, const float* base, uint32_t w, uint32_t h, uint32_t block) {
+    cuuint64_t const dims[2] = {w, h};
+    cuuint64_t const strides[1] = {static_cast<cuuint64_t>(w) * sizeof(float)};
+    cuuint32_t const box[2] = {block + 8, block + 2};
+    cuuint32_t const estr[2] = {1, 1};
+    CUresult const r = ctx->encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
+                                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+uint32_t bytes_per_solve(uint32_t b) {
+    // speed read (B^2) + time tile with its edge halo (no corners) read + time write, FP32
+    return 4u * b * b + 4u * ((b + 2u) * (b + 2u) - 4u) + 4u * b * b;
+}
+
+int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t w, uint32_t h, float spacing,
+              const uint32_t* d_seeds, uint32_t n_seeds, float* d_time, cudaStream_t st, ghcm_stats* stats) {
+    uint32_t const B = ctx->cfg.block_size;
+    uint32_t const tx = (w + B - 1) / B, ty = (h + B - 1) / B;
+    uint64_t const tiles64 = static_cast<uint64_t>(tx) * ty;
+    if (tiles64 >= (1ull << 31)) return GHCM_ERR_UNSUPPORTED;
+    uint32_t const tiles = static_cast<uint32_t>(tiles64);
+    uint32_t const max_jobs = ctx->cfg.max_jobs ? ctx->cfg.max_jobs : 8u * static_cast<uint32_t>(ctx->sms);
+    uint32_t const jobs_cap = std::min(max_jobs, tiles);
+    Layout const L = layout_for(tiles, jobs_cap);
+    if (!ctx->ws.reserve(L.total)) return GHCM_ERR_OOM;
+    char* base = ctx->ws.as<char>();
+
+    Sched s;
+    std::memset(&s, 0, sizeof(s));
+    Inst& I = *ctx->h_inst;
+    std::memset(&I, 0, sizeof(I));
+    I.in = d_field;
+    I.time = d_time;
+    I.w = w;
+    I.h = h;
+    I.tiles_x = tx;
+    I.tiles_y = ty;
+    I.tile_base = 0;
+    I.spacing = spacing;
+    I.in_is_speed = input_is_speed ? 1u : 0u;
+    bool const aligned = (w % 4u == 0u) && (reinterpret_cast<uintptr_t>(d_field) % 16u == 0u) &&
+                         (reinterpret_cast<uintptr_t>(d_time) % 16u == 0u);
+    I.tma = 0;
+    if (ctx->cfg.use_tma && ctx->encode && aligned && encode_map(ctx, &s.tmap_time, d_time, w, h, B) &&
+        encode_map(ctx, &s.tmap_in, d_field, w, h, B))
+        I.tma = 1;
+
+    s.insts = reinterpret_cast<const Inst*>(base + L.insts);
+    s.tile_inst = nullptr;
+    s.flags = reinterpret_cast<uint32_t*>(base + L.flags);
+    s.key = reinterpret_cast<uint32_t*>(base + L.key);
+    s.tmin = reinterpret_cast<float*>(base + L.tmin);
+    s.list[0] = reinterpret_cast<uint32_t*>(base + L.list0);
+    s.list[1] = reinterpret_cast<uint32_t*>(base + L.list1);
+    s.jobs = reinterpret_cast<uint32_t*>(base + L.jobs);
+    s.ctl = reinterpret_cast<Ctl*>(base + L.ctl);
+    s.num_tiles = tiles;
+    s.num_insts = 1;
+    s.max_jobs = max_jobs;
+    s.key_mode = ctx->cfg.key_mode;
+    s.max_sweeps = ctx->cfg.max_sweeps ? ctx->cfg.max_sweeps : 4u * B * B;
+    s.max_waves = ctx->cfg.max_waves;
+    s.eps = ctx->cfg.eps;
+    s.timeout_ns = static_cast<uint64_t>(ctx->cfg.wait_timeout_ms ? ctx->cfg.wait_timeout_ms : 2000u) * 1000000ull;
+
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(base + L.insts, &I, sizeof(Inst), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return map_cuda(e);
+    if ((e = cudaMemsetAsync(s.ctl, 0, sizeof(Ctl), st)) != cudaSuccess) return map_cuda(e);
+    cudaEventRecord(ctx->ev0, st);
+    if ((e = launch_init(s, &I, 1, d_seeds, nullptr, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
+        return map_cuda(e);
+    int const grid = ctx->launch.blocks_per_sm * ctx->sms;
+    if ((e = launch_persistent(static_cast<int>(B), ctx->cfg.kernel == GHCM_KERNEL_FIM, s, grid, st)) != cudaSuccess)
+        return map_cuda(e);
+    cudaEventRecord(ctx->ev1, st);
+    if ((e = cudaMemcpyAsync(ctx->h_ctl, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return map_cuda(e);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return map_cuda(e);
+
+    Ctl const& c = *ctx->h_ctl;
+#ifdef GHCM_PROFILE
+    std::fprintf(stderr,
+                 "[ghcm-prof] grid %d solves %llu waves %u barrier_ns %llu solve_ns %llu select_ns %llu sweeps %llu "
+                 "residual_ns %llu kernel_ns %llu\n",
+                 grid, c.block_solves, c.waves, c.prof[0], c.prof[1], c.prof[2], c.prof[3], c.prof[4], c.prof[5]);
+#endif
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        stats->block_solves = c.block_solves;
+        stats->cells = static_cast<uint64_t>(w) * h;
+        stats->bytes_alg = c.block_solves * static_cast<uint64_t>(bytes_per_solve(B));
+        stats->waves = c.waves;
+        stats->residual_passes = c.residual_passes;
+        stats->max_active = c.max_active;
+        stats->tiles = tiles;
+        stats->device_ms = ms;
+    }
+    if (c.error & kErrBadSeed) return GHCM_ERR_BAD_ARG;
+    if (c.error & kErrBadInput) return GHCM_ERR_BAD_INPUT;
+    if (c.error & kErrTimeout) return GHCM_ERR_TIMEOUT;
+    if (c.error & kErrInternal) return GHCM_ERR_INTERNAL;
+    if (c.error & kErrNotConverged) return GHCM_ERR_NOT_CONVERGED;
+    return GHCM_OK;
+}
+
+int check_field_args(ghcm_ctx* ctx, const void* field, uint32_t w, uint32_t h, float spacing, const void* seeds,
+                     uint32_t n_seeds, const void* out) {
+    if (!ctx || !field || !out || w == 0 || h == 0) return GHCM_ERR_BAD_ARG;
+    if (n_seeds && !seeds) return GHCM_ERR_BAD_ARG;
+    if (!(spacing > 0.f) || !std::isfinite(spacing)) return GHCM_ERR_BAD_ARG;
+    if (static_cast<uint64_t>(w) * h > (1ull << 34)) return GHCM_ERR_UNSUPPORTED;
+    return GHCM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ghcm_abi_version(void) { return GHCM_ABI_VERSION; }
+
+const char* ghcm_status_string(int status) {
+    switch (status) {
+        case GHCM_OK: return "ok";
+        case GHCM_ERR_BAD_ARG: return "bad argument";
+        case GHCM_ERR_BAD_INPUT: return "input field holds a NaN or negative value";
+        case GHCM_ERR_OOM: return "out of memory";
+        case GHCM_ERR_CUDA: return "CUDA error";
+        case GHCM_ERR_TIMEOUT: return "a bounded device wait timed out";
+        case GHCM_ERR_NOT_CONVERGED: return "wave cap reached before convergence";
+        case GHCM_ERR_UNSUPPORTED: return "unsupported device or size";
+        case GHCM_ERR_INTERNAL: return "internal error";
+        default: return "unknown status";
+    }
+}
+
+int ghcm_config_default(ghcm_config* cfg) {
+    if (!cfg) return GHCM_ERR_BAD_ARG;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->block_size = 16;
+    cfg->max_jobs = 0;
+    cfg->eps = 1e-5f;
+    cfg->kernel = GHCM_KERNEL_SYSTOLIC;
+    cfg->schedule = GHCM_SCHEDULE_PLAIN;
+    cfg->key_mode = GHCM_KEY_BOUNDARY_MIN;
+    cfg->max_sweeps = 0;
+    cfg->max_waves = 0;
+    cfg->wait_timeout_ms = 2000;
+    cfg->device = -1;
+    cfg->use_tma = 1;
+    return GHCM_OK;
+}
+
+int ghcm_create(const ghcm_config* cfg, ghcm_ctx** out) {
+    if (!out) return GHCM_ERR_BAD_ARG;
+    *out = nullptr;
+    int rc = check_config(cfg);
+    if (rc != GHCM_OK) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return GHCM_ERR_UNSUPPORTED;
+    }
+    int dev = cfg->device;
+    if (dev < 0 && cudaGetDevice(&dev) != cudaSuccess) return GHCM_ERR_CUDA;
+    if (dev >= ndev) return GHCM_ERR_BAD_ARG;
+    if (cudaSetDevice(dev) != cudaSuccess) return GHCM_ERR_CUDA;
+    int coop = 0, sms = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (!coop || sms <= 0) return GHCM_ERR_UNSUPPORTED;
+
+    ghcm_ctx* ctx = new (std::nothrow) ghcm_ctx();
+    if (!ctx) return GHCM_ERR_OOM;
+    ctx->cfg = *cfg;
+    ctx->device = dev;
+    ctx->sms = sms;
+    if (query_persistent(static_cast<int>(cfg->block_size), cfg->kernel == GHCM_KERNEL_FIM, &ctx->launch) != 0 ||
+        ctx->launch.blocks_per_sm <= 0) {
+        delete ctx;
+        return GHCM_ERR_UNSUPPORTED;
+    }
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+        ctx->encode = reinterpret_cast<EncodeTiledFn>(fn);
+    else
+        cudaGetLastError();
+    if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+        cudaMallocHost(reinterpret_cast<void**>(&ctx->h_inst), sizeof(Inst)) != cudaSuccess ||
+        cudaMallocHost(reinterpret_cast<void**>(&ctx->h_ctl), sizeof(Ctl)) != cudaSuccess) {
+        ghcm_destroy(ctx);
+        return GHCM_ERR_OOM;
+    }
+    *out = ctx;
+    return GHCM_OK;
+}
+
+int ghcm_destroy(ghcm_ctx* ctx) {
+    if (!ctx) return GHCM_OK;
+    cudaSetDevice(ctx->device);
+    ctx->ws.release();
+    ctx->d_in.release();
+    ctx->d_time.release();
+    ctx->d_seeds.release();
+    if (ctx->h_inst) cudaFreeHost(ctx->h_inst);
+    if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    delete ctx;
+    return GHCM_OK;
+}
+
+int ghcm_device_sm_count(const ghcm_ctx* ctx, uint32_t* out) {
+    if (!ctx || !out) return GHCM_ERR_BAD_ARG;
+    *out = static_cast<uint32_t>(ctx->sms);
+    return GHCM_OK;
+}
+
+int ghcm_solve_device(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t width, uint32_t height,
+                      float h, const uint32_t* d_seeds_xy, uint32_t n_seeds, float* d_time_out, void* stream,
+                      ghcm_stats* stats) {
+    int rc = check_field_args(ctx, d_field, width, height, h, d_seeds_xy, n_seeds, d_time_out);
+    if (rc != GHCM_OK) return rc;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return GHCM_ERR_CUDA;
+    auto const t0 = std::chrono::steady_clock::now();
+    rc = run_solve(ctx, d_field, input_is_speed, width, height, h, d_seeds_xy, n_seeds, d_time_out,
+                   static_cast<cudaStream_t>(stream), stats);
+    if (stats) stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int ghcm_solve(ghcm_ctx* ctx, const float* field, int input_is_speed, uint32_t width, uint32_t height, float h,
+               const uint32_t* seeds_xy, uint32_t n_seeds, float* time_out, ghcm_stats* stats) {
+    int rc = check_field_args(ctx, field, width, height, h, seeds_xy, n_seeds, time_out);
+    if (rc != GHCM_OK) return rc;
+    for (uint32_t i = 0; i < n_seeds; ++i)
+        if (seeds_xy[2 * i] >= width || seeds_xy[2 * i + 1] >= height) return GHCM_ERR_BAD_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return GHCM_ERR_CUDA;
+    auto const t0 = std::chrono::steady_clock::now();
+    size_t const bytes = static_cast<size_t>(width) * height * sizeof(float);
+    if (!ctx->d_in.reserve(bytes) || !ctx->d_time.reserve(bytes) ||
+        !ctx->d_seeds.reserve(std::max<size_t>(8, 8ull * n_seeds)))
+        return GHCM_ERR_OOM;
+    cudaStream_t const st = nullptr;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(ctx->d_in.p, field, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return map_cuda(e);
+    if (n_seeds &&
+        (e = cudaMemcpyAsync(ctx->d_seeds.p, seeds_xy, 8ull * n_seeds, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return map_cuda(e);
+    rc = run_solve(ctx, ctx->d_in.as<float>(), input_is_speed, width, height, h, ctx->d_seeds.as<uint32_t>(),
+                   n_seeds, ctx->d_time.as<float>(), st, stats);
+    if (rc == GHCM_OK || rc == GHCM_ERR_NOT_CONVERGED) {
+        if ((e = cudaMemcpy(time_out, ctx->d_time.p, bytes, cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return map_cuda(e);
+    }
+    if (stats) stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int ghcm_selftest_wait_timeout(ghcm_ctx* ctx, uint32_t timeout_ms) {
+    if (!ctx || timeout_ms == 0 || timeout_ms > 60000) return GHCM_ERR_BAD_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return GHCM_ERR_CUDA;
+    DevBuf buf;
+    if (!buf.reserve(align_up(sizeof(Ctl), 256) + 256)) return GHCM_ERR_OOM;
+    Ctl* ctl = buf.as<Ctl>();
+    uint32_t* flag = reinterpret_cast<uint32_t*>(buf.as<char>() + align_up(sizeof(Ctl), 256));
+    cudaError_t e = cudaMemset(buf.p, 0, buf.bytes);
+    if (e == cudaSuccess) e = launch_wait_selftest(flag, ctl, static_cast<uint64_t>(timeout_ms) * 1000000ull, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    Ctl host{};
+    if (e == cudaSuccess) e = cudaMemcpy(&host, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost);
+    buf.release();
+    if (e != cudaSuccess) return map_cuda(e);
+    return (host.error & kErrTimeout) ? GHCM_ERR_TIMEOUT : GHCM_OK;
+}
+
+}  // extern "C"

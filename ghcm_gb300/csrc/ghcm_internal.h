@@ -1,0 +1,95 @@
+// Internal types shared by the C-ABI layer (ghcm_capi.cpp) and the kernels
+// (ghcm_solver.cu). Not part of the public interface.
+#pragma once
+
+#include <cstdint>
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+namespace ghcm {
+
+// Error bits written to Ctl::error by device code; the host maps them to
+// GHCM_ERR_* codes.
+enum : uint32_t {
+    kErrTimeout      = 1u << 0,  // a bounded wait ran out
+    kErrBadInput     = 1u << 1,  // NaN or negative speed / cost
+    kErrNotConverged = 1u << 2,  // wave cap reached
+    kErrInternal     = 1u << 3,  // list overflow or an impossible state
+    kErrBadSeed      = 1u << 4,  // a device-resident seed lies outside its field
+};
+
+// Per-tile scheduler flags.
+enum : uint32_t {
+    kActive   = 1u << 0,   // tile is in the active set (queued or about to be)
+    kFull     = 1u << 1,   // re-solve every cell (residual judge, sweep cap)
+    kEdgeBit0 = 1u << 4,   // edge e of the tile received new boundary values: kEdgeBit0 << e
+    kEdgeMask = 0xFu << 4,
+};
+
+// One eikonal instance: a row-major W x H field and its block tiling.
+struct Inst {
+    const float* in;       // speed (in_is_speed) or cost
+    float*       time;     // arrival times (in/out)
+    uint32_t     w, h;
+    uint32_t     tiles_x, tiles_y;
+    uint32_t     tile_base;  // first global tile id of this instance
+    float        spacing;    // h: cost = h / speed
+    uint32_t     in_is_speed;
+    int32_t      tma;        // 1: tiles of this instance are staged by TMA with the maps in Sched
+    uint32_t     cell_base_lo, cell_base_hi;  // unused by the single-grid path
+};
+
+// Device-side control block of one solve.
+struct Ctl {
+    uint32_t bar_count, bar_gen;   // grid barrier words (BarrierWords layout)
+    uint32_t error;                // kErr* bits
+    uint32_t stop;                 // 1: leave the wave loop
+    uint32_t count[2];             // sizes of the two active lists
+    uint32_t job_count;            // jobs selected for the current wave
+    uint32_t job_next;             // next job to hand out
+    uint32_t jobs_in_list;         // 1: jobs are list[cur] itself; 0: the jobs array
+    uint32_t waves;
+    uint32_t residual_passes;
+    uint32_t max_active;
+    unsigned long long block_solves;
+    unsigned long long prof[8];    // GHCM_PROFILE builds: per-phase nanoseconds and sweep counts
+};
+
+// Everything the persistent kernel needs; passed by value as a
+// __grid_constant__ parameter so that the tensor maps sit in parameter space.
+struct Sched {
+    CUtensorMap tmap_time;         // box (B+8) x (B+2) over the time field of instance 0
+    CUtensorMap tmap_in;           // same box over the speed/cost field of instance 0
+    const Inst* insts;
+    const uint32_t* tile_inst;     // per-tile instance index (nullptr: a single instance)
+    uint32_t* flags;               // per-tile kActive | kFull | edge bits
+    uint32_t* key;                 // per-tile priority key (float bits; +inf = none)
+    float*    tmin;                // per-tile smallest time after the last solve
+    uint32_t* list[2];             // active lists, capacity num_tiles each
+    uint32_t* jobs;                // selected jobs, capacity max_jobs
+    Ctl*      ctl;
+    uint32_t  num_tiles;
+    uint32_t  num_insts;
+    uint32_t  max_jobs;
+    uint32_t  key_mode;
+    uint32_t  max_sweeps;
+    uint32_t  max_waves;
+    float     eps;
+    uint32_t  pad0;
+    uint64_t  timeout_ns;
+};
+
+// Launch configuration chosen by the host for a (block size, kernel) pair.
+struct LaunchInfo {
+    int threads;
+    int blocks_per_sm;
+};
+
+// Host entry points implemented in ghcm_solver.cu.
+int query_persistent(int block, int fim, LaunchInfo* info);
+cudaError_t launch_init(const Sched& s, const Inst* h_insts, uint32_t n_insts, const uint32_t* d_seeds,
+                        const uint32_t* d_seed_inst, uint32_t n_seeds, int block, cudaStream_t st);
+cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cudaStream_t st);
+cudaError_t launch_wait_selftest(uint32_t* flag, Ctl* ctl, uint64_t timeout_ns, cudaStream_t st);
+
+}  // namespace ghcm

@@ -1,0 +1,134 @@
+/*
+ * ghcm.h - C ABI of the GB300 gHCM eikonal solver (libghcm.so).
+ *
+ * Replaces the reference's solver interface src/eikonal.h:12-67 for the gHCM
+ * path (HcmConfig, EikonalResult, eikonal_hcm_opencl{,_setup,_ex}); the block
+ * scheduler of src/eikonal_hcm.cpp:186-529 and the tile kernels of
+ * data/eikonal_ghcm_systolic.cl / data/eikonal_ghcm_fim.cl run on the device.
+ *
+ * Plain C: pointers and sizes only. Every call returns an int status
+ * (GHCM_OK or a negative GHCM_ERR_*); nothing exits or throws across the ABI,
+ * unlike the reference's cl_do/exit paths (src/util_opencl.h:48-57,
+ * src/eikonal_hcm.cpp:181-182).
+ *
+ * Fields are row-major float32 with x fastest: cell (x, y) is element
+ * x + y * width (src/util_dim.h:17-21). Seeds are width/height-bounded
+ * (x, y) pairs of uint32 with arrival time 0.
+ *
+ * Threading: a context may be used by one host thread at a time; calls on a
+ * context are serialised. Different contexts are independent.
+ */
+#ifndef GHCM_H
+#define GHCM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GHCM_ABI_VERSION 1
+
+/* status codes */
+#define GHCM_OK                 0
+#define GHCM_ERR_BAD_ARG       -1  /* null pointer, zero size, seed outside the field, bad config */
+#define GHCM_ERR_BAD_INPUT     -2  /* a speed/cost value is NaN or negative */
+#define GHCM_ERR_OOM           -3  /* device or pinned allocation failed */
+#define GHCM_ERR_CUDA          -4  /* a CUDA runtime call failed */
+#define GHCM_ERR_TIMEOUT       -5  /* a bounded device-side wait ran out */
+#define GHCM_ERR_NOT_CONVERGED -6  /* the wave cap was reached before convergence */
+#define GHCM_ERR_UNSUPPORTED   -7  /* no usable GPU, or a size the build does not support */
+#define GHCM_ERR_INTERNAL      -8  /* an internal invariant failed (a bug) */
+
+/* ghcm_config.kernel - the tile solver (HcmConfig::Kernel, src/eikonal.h:13) */
+#define GHCM_KERNEL_SYSTOLIC 0     /* sweep every cell until the tile converges */
+#define GHCM_KERNEL_FIM      1     /* block-FIM: open-set cells only */
+
+/* ghcm_config.schedule */
+#define GHCM_SCHEDULE_PLAIN   0    /* lowest-key-first top-n (the reference's priority queue) */
+#define GHCM_SCHEDULE_LEARNED 1    /* learned block-scheduling score */
+
+/* ghcm_config.key_mode - the plain priority key */
+#define GHCM_KEY_BOUNDARY_MIN 0    /* min arrival time among the boundary values that activated the tile */
+#define GHCM_KEY_BLOCK_MIN    1    /* min smallest_time over the tile and its 4 neighbours
+                                      (BlockWrapper::calc_min_time, src/eikonal_hcm.cpp:58-70) */
+
+typedef struct ghcm_config {
+    uint32_t block_size;      /* tile side: 8, 16 or 32 (HcmConfig::block_size) */
+    uint32_t max_jobs;        /* n, tiles solved per wave; 0 = 8 x SM count
+                                 (HcmConfig::compute_unit_overload x compute units) */
+    float    eps;             /* convergence threshold on |dT| (HcmConfig::fim_minimum_change) */
+    uint32_t kernel;          /* GHCM_KERNEL_* */
+    uint32_t schedule;        /* GHCM_SCHEDULE_* */
+    uint32_t key_mode;        /* GHCM_KEY_* */
+    uint32_t max_sweeps;      /* cap on inner sweeps per block-solve; 0 = 4 * block_size^2 */
+    uint32_t max_waves;       /* cap on waves per solve; 0 = no cap */
+    uint32_t wait_timeout_ms; /* limit of every device-side wait; 0 = 2000 */
+    int32_t  device;          /* CUDA device ordinal; -1 = the current device */
+    uint32_t use_tma;         /* 1 = stage tiles with TMA when the field allows it; 0 = plain loads */
+    uint32_t reserved[5];     /* must be zero */
+} ghcm_config;
+
+typedef struct ghcm_stats {
+    uint64_t block_solves;    /* tile dispatches (the reference's profiling_info.size()) */
+    uint64_t cells;           /* total cells solved for */
+    uint64_t bytes_alg;       /* block_solves x algorithmic bytes per block-solve */
+    uint32_t waves;           /* scheduler iterations */
+    uint32_t residual_passes; /* global residual checks run */
+    uint32_t max_active;      /* largest active-tile set seen */
+    uint32_t tiles;           /* tiles in the tiling */
+    double   device_ms;       /* device time from device-resident input to converged field */
+    double   total_ms;        /* host wall time of the call, copies included */
+} ghcm_stats;
+
+typedef struct ghcm_ctx ghcm_ctx;
+
+/* Fills *cfg with the defaults (HcmConfig defaults, src/eikonal.h:17-26,
+ * except block_size 16 and max_jobs 0). */
+int ghcm_config_default(ghcm_config* cfg);
+
+/* Creates a solver context on cfg->device. Replaces
+ * eikonal_hcm_opencl_setup (src/eikonal_hcm.cpp:137-175). */
+int ghcm_create(const ghcm_config* cfg, ghcm_ctx** out);
+
+/* Releases a context and all its device memory. NULL is accepted. */
+int ghcm_destroy(ghcm_ctx* ctx);
+
+/* Solves for the arrival-time field with host buffers. Replaces
+ * eikonal_hcm_opencl_ex (src/eikonal_hcm.cpp:186-529).
+ *   field:      width*height values, speed (input_is_speed = 1, cost = h / speed)
+ *               or cost (input_is_speed = 0, as the reference takes it)
+ *   seeds_xy:   n_seeds (x, y) pairs
+ *   time_out:   width*height arrival times (written)
+ *   stats:      optional */
+int ghcm_solve(ghcm_ctx* ctx, const float* field, int input_is_speed, uint32_t width, uint32_t height,
+               float h, const uint32_t* seeds_xy, uint32_t n_seeds, float* time_out, ghcm_stats* stats);
+
+/* Same with device-resident buffers on `stream` (a cudaStream_t; NULL = the
+ * legacy default stream). d_seeds_xy is a device array. Returns when the
+ * solve has finished on the stream. */
+int ghcm_solve_device(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t width,
+                      uint32_t height, float h, const uint32_t* d_seeds_xy, uint32_t n_seeds,
+                      float* d_time_out, void* stream, ghcm_stats* stats);
+
+/* Number of SMs of the context's device (the reference's compute units). */
+int ghcm_device_sm_count(const ghcm_ctx* ctx, uint32_t* out);
+
+/* Human-readable text for a status code. Never NULL. */
+const char* ghcm_status_string(int status);
+
+/* ABI version (GHCM_ABI_VERSION). */
+int ghcm_abi_version(void);
+
+/* Self-test of the bounded-wait path: launches a kernel that waits on a flag
+ * nothing sets, with a limit of timeout_ms, and returns its status
+ * (GHCM_ERR_TIMEOUT when the limit works). No counterpart in the reference,
+ * whose device asserts spin forever (data/util_common.cl:26-30). */
+int ghcm_selftest_wait_timeout(ghcm_ctx* ctx, uint32_t timeout_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GHCM_H */

@@ -1,0 +1,98 @@
+"""The CPU oracle against the reference: bit-exact on the golden fixtures the
+reference itself produced, and on fresh seeded fields against the reference
+build where its sources are present. No GPU needed."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+from ghcm_gb300 import fields
+from oracle.oracle import REF_SO, Reference, build, reference_available, rel_diff
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_fim_matches_reference_golden(oracle_lib, name):
+    g = load_golden(name)
+    out5, _ = oracle_lib.fim(g["cost"], g["seeds"], 1e-5)
+    out3, _ = oracle_lib.fim(g["cost"], g["seeds"], 1e-3)
+    np.testing.assert_array_equal(out5, g["fim_1e5"])
+    np.testing.assert_array_equal(out3, g["fim_1e3"])
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_fmm_matches_reference_golden(oracle_lib, name):
+    g = load_golden(name)
+    out, _ = oracle_lib.fmm(g["cost"], g["seeds"])
+    np.testing.assert_array_equal(out, g["fmm"])
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_fmm64_close_to_fp32(oracle_lib, name):
+    g = load_golden(name)
+    d, _ = oracle_lib.fmm64(g["cost"], g["seeds"])
+    assert rel_diff(g["fmm"], d) < 1e-5
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_golden_fim_is_a_fixed_point(oracle_lib, name):
+    g = load_golden(name)
+    # every cell is within eps of its own Godunov update (the FIM stop rule)
+    assert oracle_lib.residual(g["cost"], g["fim_1e5"]) <= 1e-5
+    for s in g["seeds"]:
+        assert g["fim_1e5"][s[1], s[0]] == 0.0
+
+
+def test_constant_field_axis_distances(oracle_lib):
+    g = load_golden("constant_33x17")
+    sx, sy = g["seeds"][0]
+    t = g["fim_1e5"]
+    # along the seed's row and column the Godunov solution is the exact L1 distance
+    np.testing.assert_array_equal(t[sy, :], np.abs(np.arange(33) - sx).astype(np.float32))
+    np.testing.assert_array_equal(t[:, sx], np.abs(np.arange(17) - sy).astype(np.float32))
+
+
+def test_unreachable_cells_stay_infinite(oracle_lib):
+    g = load_golden("walls_inf_40")
+    t = g["fim_1e5"]
+    assert np.all(np.isinf(t[np.isinf(g["cost"])]) | (t[np.isinf(g["cost"])] == 0))
+    assert np.isfinite(t).any() and np.isinf(t).any()
+
+
+@pytest.mark.skipif(not reference_available(), reason="reference sources not present")
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_restatement_bit_exact_vs_reference_build(oracle_lib, seed):
+    if not REF_SO.exists():
+        build(with_reference=True)
+    ref = Reference()
+    rng = np.random.default_rng(seed)
+    h, w = int(rng.integers(20, 90)), int(rng.integers(20, 90))
+    speed, seeds = fields.value_noise(h, seed=seed, base_period=12.0, sources=int(rng.integers(1, 5)), w=w)
+    speed[rng.random(speed.shape) < 0.05] = 0.0  # sprinkle impassable cells
+    cost = fields.cost_from_speed(speed)
+    for eps in (1e-5, 1e-3, 0.0):
+        np.testing.assert_array_equal(oracle_lib.fim(cost, seeds, eps)[0], ref.fim(cost, seeds, eps)[0])
+    np.testing.assert_array_equal(oracle_lib.fmm(cost, seeds)[0], ref.fmm(cost, seeds)[0])
+
+
+def test_fim_vs_fmm_agree_on_ring(oracle_lib):
+    speed, seeds = fields.ring7_small(1)
+    cost = fields.cost_from_speed(speed)
+    a, _ = oracle_lib.fim(cost, seeds, 1e-5)
+    b, _ = oracle_lib.fmm(cost, seeds)
+    assert rel_diff(a, b) < 1e-5
+
+
+def test_oracle_rejects_bad_arguments(oracle_lib):
+    cost = np.ones((4, 4), dtype=np.float32)
+    with pytest.raises(ValueError):
+        oracle_lib.fim(cost, np.array([[4, 0]], dtype=np.uint32))
+    with pytest.raises(ValueError):
+        oracle_lib.fmm(cost, np.array([[0, 9]], dtype=np.uint32))
+
+
+def test_rel_diff_conventions():
+    inf = np.float32(np.inf)
+    assert rel_diff(np.array([inf, 1.0]), np.array([inf, 1.0])) == 0.0
+    assert rel_diff(np.array([1.0, 2.0]), np.array([inf, 2.0])) == float("inf")
+    assert abs(rel_diff(np.array([0.0, 2.0 + 2e-6]), np.array([0.0, 2.0])) - 1e-6) < 1e-9
