@@ -65,6 +65,7 @@ class GhcmStats(ctypes.Structure):
         ("tiles", ctypes.c_uint32),
         ("device_ms", ctypes.c_double),
         ("total_ms", ctypes.c_double),
+        ("kernel_ms", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:

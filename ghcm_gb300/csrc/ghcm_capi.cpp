@@ -61,7 +61,7 @@ struct ghcm_ctx {
     int sms = 0;
     LaunchInfo launch{};
     EncodeTiledFn encode = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     // scheduler workspace: flags | key | tmin | list0 | list1 | jobs | ctl | insts
     DevBuf ws;
     // field buffers used by ghcm_solve (host-pointer entry)
@@ -117,7 +117,9 @@ Layout layout_for(uint32_t tiles, uint32_t jobs) {
 bool encode_map(ghcm_ctx* ctx, CUtensorMap* map, const float* base, uint32_t w, uint32_t h, uint32_t block) {
     cuuint64_t const dims[2] = {w, h};
     cuuint64_t const strides[1] = {static_cast<cuuint64_t>(w) * sizeof(float)};
-    cuuint32_t const box[2] = {block + 8, block + 2};
+    uint32_t bw = 0, bh = 0;
+    tile_box(static_cast<int>(block), &bw, &bh);  // the tile with its halo, x from ox-4 (16-byte aligned)
+    cuuint32_t const box[2] = {bw, bh};
     cuuint32_t const estr[2] = {1, 1};
     CUresult const r = ctx->encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
                                    box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -189,6 +191,7 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     if ((e = launch_init(s, &I, 1, d_seeds, nullptr, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
         return map_cuda(e);
     int const grid = ctx->launch.blocks_per_sm * ctx->sms;
+    cudaEventRecord(ctx->ev2, st);
     if ((e = launch_persistent(static_cast<int>(B), ctx->cfg.kernel == GHCM_KERNEL_FIM, s, grid, st)) != cudaSuccess)
         return map_cuda(e);
     cudaEventRecord(ctx->ev1, st);
@@ -199,13 +202,16 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     Ctl const& c = *ctx->h_ctl;
 #ifdef GHCM_PROFILE
     std::fprintf(stderr,
-                 "[ghcm-prof] grid %d solves %llu waves %u barrier_ns %llu solve_ns %llu select_ns %llu sweeps %llu "
+                 "[ghcm-prof] grid %d solves %llu waves %u residual_passes %u barrier_ns %llu solve_ns %llu sweeps %llu "
                  "residual_ns %llu kernel_ns %llu\n",
-                 grid, c.block_solves, c.waves, c.prof[0], c.prof[1], c.prof[2], c.prof[3], c.prof[4], c.prof[5]);
+                 grid, c.block_solves, c.waves, c.residual_passes, c.prof[0], c.prof[1], c.prof[3], c.prof[4],
+                 c.prof[5]);
 #endif
     if (stats) {
-        float ms = 0.f;
+        float ms = 0.f, kms = 0.f;
         cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        cudaEventElapsedTime(&kms, ctx->ev2, ctx->ev1);
+        stats->kernel_ms = kms;
         stats->block_solves = c.block_solves;
         stats->cells = static_cast<uint64_t>(w) * h;
         stats->bytes_alg = c.block_solves * static_cast<uint64_t>(bytes_per_solve(B));
@@ -307,6 +313,7 @@ int ghcm_create(const ghcm_config* cfg, ghcm_ctx** out) {
     else
         cudaGetLastError();
     if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev2) != cudaSuccess ||
         cudaMallocHost(reinterpret_cast<void**>(&ctx->h_inst), sizeof(Inst)) != cudaSuccess ||
         cudaMallocHost(reinterpret_cast<void**>(&ctx->h_ctl), sizeof(Ctl)) != cudaSuccess) {
         ghcm_destroy(ctx);
@@ -327,6 +334,7 @@ int ghcm_destroy(ghcm_ctx* ctx) {
     if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->ev2) cudaEventDestroy(ctx->ev2);
     delete ctx;
     return GHCM_OK;
 }

@@ -43,10 +43,10 @@ struct Inst {
 struct Ctl {
     uint32_t bar_count, bar_gen;   // grid barrier words (BarrierWords layout)
     uint32_t error;                // kErr* bits
-    uint32_t stop;                 // 1: leave the wave loop
+    uint32_t phase;                // scheduler phase (kPhase*)
+    uint32_t cur;                  // list the current jobs come from; activations go to list[cur ^ 1]
     uint32_t count[2];             // sizes of the two active lists
     uint32_t job_count;            // jobs selected for the current wave
-    uint32_t job_next;             // next job to hand out
     uint32_t jobs_in_list;         // 1: jobs are list[cur] itself; 0: the jobs array
     uint32_t waves;
     uint32_t residual_passes;
@@ -87,6 +87,8 @@ struct LaunchInfo {
 
 // Host entry points implemented in ghcm_solver.cu.
 int query_persistent(int block, int fim, LaunchInfo* info);
+// The staged box (elements) of a tile: the TMA tensor maps use it as their box.
+void tile_box(int block, uint32_t* width, uint32_t* height);
 cudaError_t launch_init(const Sched& s, const Inst* h_insts, uint32_t n_insts, const uint32_t* d_seeds,
                         const uint32_t* d_seed_inst, uint32_t n_seeds, int block, cudaStream_t st);
 cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cudaStream_t st);

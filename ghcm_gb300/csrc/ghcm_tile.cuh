@@ -1,0 +1,371 @@
+// Block-solves, one tile per CTA.
+//
+// A CTA stages its tile with a two-cell halo (time and speed/cost) into
+// shared memory - one 2-D TMA box load each, or plain loads when the field's
+// layout does not allow TMA - and every thread owns one (B <= 16) or four
+// (B = 32) cells of the tile.
+//
+//   systolic  every sweep updates the cells in place (each thread its own,
+//             reading its four neighbours from shared memory) until a sweep
+//             moves no cell by more than eps; the reference sweeps
+//             work-group-sized chunks the same way
+//             (data/eikonal_ghcm_systolic.cl:130-153). Rows whose neighbourhood
+//             did not change in the previous sweep are skipped.
+//   block-FIM only open cells are solved; a converged cell asks its in-tile
+//             neighbours to re-check and a neighbour that improves by more
+//             than eps opens (data/eikonal_ghcm_fim.cl:166-210, 347-372).
+//             The initial open set is the rows of the edges neighbours
+//             flagged (fim.cl:306-332), the cells next to seeds and, for tiles
+//             re-queued by the residual judge, every cell.
+//
+// Then each neighbour edge row is probed with the converged tile
+// (check_border, data/eikonal_ghcm_systolic.cl:8-41) - probe-only, as
+// data/eikonal_ghcm_fim.cl:175-194 does, so no tile writes into another.
+// The probe recomputes the neighbour's own update exactly: the second halo
+// ring supplies the cell beyond the probed one (the reference treats it as
+// +inf, data/eikonal_common.cl:199-206). A neighbour is activated only when
+// the probe improves it by more than eps AND this solve changed the edge row
+// facing it; with rounding the Godunov update is not monotone, and without
+// the second condition two converged tiles can keep activating each other.
+#pragma once
+
+#include "ghcm_sched.cuh"
+
+namespace ghcm {
+
+template <int B>
+struct TileGeom {
+    static constexpr int THREADS = (B * B < 64) ? 64 : (B * B > 256 ? 256 : B * B);
+    static constexpr int CPT = (B * B) / THREADS;  // cells per thread
+    static constexpr int ROWS_PER_PASS = THREADS / B;
+    static constexpr int BW = B + 8;               // staged box width: x in [ox-4, ox+B+4), 16-byte aligned start
+    static constexpr int BH = B + 4;               // staged box height: y in [oy-2, oy+B+2)
+    static constexpr int BOX = BW * BH;
+    static constexpr int BOXP = (BOX + 31) / 32 * 32;  // keeps each box 128-byte aligned for TMA
+    static constexpr int RING = (B + 4) * (B + 4);      // the tile and its two halo rings
+    static_assert(4 * B % 32 == 0, "edge probes need whole warps");
+    static_assert(B * B % THREADS == 0, "cells must divide evenly");
+    static_assert(B <= 32, "row masks are 32 bits");
+};
+
+template <int B>
+struct alignas(128) TileSmem {
+    float time[TileGeom<B>::BOXP];
+    float cost[TileGeom<B>::BOXP];
+    uint8_t check[B * B];  // block-FIM: re-check requests
+};
+
+// index of local cell (x, y), x in [-4, B+4), y in [-2, B+2), in a staged box
+template <int B>
+__device__ __forceinline__ int si(int x, int y) {
+    return (y + 2) * TileGeom<B>::BW + x + 4;
+}
+
+// One block-solve of `tile`; activations go to list[nxt]. Returns false if
+// the TMA stage timed out (the grid then stops at the next barrier).
+template <int B, bool FIM>
+__device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<B>& sm, uint64_t* bar,
+                           uint32_t& parity, bool& tma_pending, uint32_t* s_word, float* s_red) {
+    using G = TileGeom<B>;
+    int const tid = threadIdx.x;
+    const Inst& I = s.insts[inst_of(s, tile)];
+    TileCoord const tc = tile_coord<B>(I, tile);
+    bool const use_tma = I.tma != 0;
+
+    // Claim: clear the tile's activation state (a later activation re-queues
+    // it), then stage the tile with its halo.
+    if (tid == 0) {
+        uint32_t const f = atomicAnd(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
+        atomicExch(&s.key[tile], inf_bits());
+        __threadfence();
+        s_word[0] = f;
+        s_word[1] = 0u;  // abort flag
+        s_word[4] = 0u;           // edge rows changed by this solve
+        s_word[5] = 0xffffffffu;  // rows changed, by sweep mod 3: sweep k reads [5 + k%3],
+        s_word[6] = 0u;           // writes [5 + (k+1)%3] and clears [5 + (k+2)%3];
+        s_word[7] = 0u;           // the first sweep evaluates every row
+        if (use_tma) {
+            fence_proxy_async();
+            mbar_arrive_expect_tx(bar, static_cast<uint32_t>(2 * G::BOX * sizeof(float)));
+            tma_load_2d(sm.time, &s.tmap_time, bar, tc.ox - 4, tc.oy - 2);
+            tma_load_2d(sm.cost, &s.tmap_in, bar, tc.ox - 4, tc.oy - 2);
+            tma_pending = true;
+        }
+    }
+    __syncthreads();
+    uint32_t const flags = s_word[0];
+    if (use_tma) {
+        if (!mbar_wait(bar, parity, s.timeout_ns)) {
+            atomicOr(&s.ctl->error, kErrTimeout);
+            s_word[1] = 1u;  // every thread acts on it after the barrier below
+        } else if (tid == 0) {
+            tma_pending = false;
+        }
+        parity ^= 1u;
+    }
+    // fill / fix up the two rings: outside the field is +inf; speed -> cost
+    for (int r = tid; r < G::RING; r += G::THREADS) {
+        int const lx = r % (B + 4) - 2, ly = r / (B + 4) - 2;
+        int const gx = tc.ox + lx, gy = tc.oy + ly;
+        int const k = si<B>(lx, ly);
+        bool const in = gx >= 0 && gy >= 0 && gx < static_cast<int>(I.w) && gy < static_cast<int>(I.h);
+        if (!in) {
+            sm.time[k] = f_inf();
+            sm.cost[k] = f_inf();
+        } else if (use_tma) {
+            if (I.in_is_speed) sm.cost[k] = __fdiv_rn(I.spacing, sm.cost[k]);
+        } else {
+            size_t const gi = static_cast<size_t>(gy) * I.w + gx;
+            sm.time[k] = __ldcg(&I.time[gi]);
+            sm.cost[k] = to_cost(I, __ldg(&I.in[gi]));
+        }
+    }
+    __syncthreads();
+    if (s_word[1]) return false;
+
+    constexpr int BW = G::BW;
+    float t[G::CPT], t0[G::CPT], c[G::CPT], c2[G::CPT];
+    int idx[G::CPT], lxs[G::CPT], lys[G::CPT];
+    bool v[G::CPT], inside[G::CPT];
+#pragma unroll
+    for (int k = 0; k < G::CPT; ++k) {
+        int const id = tid + k * G::THREADS;
+        lxs[k] = id % B;
+        lys[k] = id / B;
+        inside[k] = lxs[k] < tc.sx && lys[k] < tc.sy;
+        idx[k] = si<B>(lxs[k], lys[k]);
+        t[k] = sm.time[idx[k]];
+        t0[k] = t[k];
+        c[k] = sm.cost[idx[k]];
+        c2[k] = __fmul_rn(__fmul_rn(c[k], c[k]), 2.0f);
+        v[k] = inside[k] && c[k] < f_inf();
+    }
+    float const eps = s.eps;
+    bool own_changed = false;
+    bool capped = false;
+    uint32_t sweeps = 0;
+
+    if (!FIM) {
+        for (;;) {
+            uint32_t const rd = sweeps % 3u;
+            uint32_t const rows = s_word[5 + rd];
+            bool moved = false;
+            uint32_t my_rows = 0u;
+#pragma unroll
+            for (int k = 0; k < G::CPT; ++k) {
+                int const y = lys[k];
+                uint32_t const near = (1u << y) | (y > 0 ? 1u << (y - 1) : 0u) | (y + 1 < B ? 1u << (y + 1) : 0u);
+                if (!v[k] || !(rows & near)) continue;
+                int const i = idx[k];
+                float const ax = fminf(sm.time[i - 1], sm.time[i + 1]);
+                float const ay = fminf(sm.time[i - BW], sm.time[i + BW]);
+                float const nt = godunov2(ax, ay, c[k], c2[k], t[k]);
+                if (nt < t[k]) {
+                    moved |= time_diff(nt, t[k]) < -eps;
+                    t[k] = nt;
+                    sm.time[i] = nt;
+                    own_changed = true;
+                    my_rows |= 1u << y;
+                }
+            }
+            // rows changed in this sweep: one shared atomic per warp
+            my_rows = __reduce_or_sync(0xffffffffu, my_rows);
+            if ((tid & 31) == 0 && my_rows) atomicOr(&s_word[5 + (rd + 1u) % 3u], my_rows);
+            if (tid == 0) s_word[5 + (rd + 2u) % 3u] = 0u;
+            ++sweeps;
+            if (!__syncthreads_or(moved)) break;
+            if (sweeps >= s.max_sweeps) {
+                capped = true;
+                break;
+            }
+        }
+    } else {
+        uint8_t* check = sm.check;
+        bool open[G::CPT];
+        uint32_t const edges = (flags & kEdgeMask) >> 4;
+        bool const full = (flags & kFull) != 0u;
+#pragma unroll
+        for (int k = 0; k < G::CPT; ++k) {
+            int const i = idx[k];
+            bool const on_edge = ((edges & 1u) && lxs[k] == 0) || ((edges & 2u) && lys[k] == 0) ||
+                                 ((edges & 4u) && lxs[k] == tc.sx - 1) || ((edges & 8u) && lys[k] == tc.sy - 1);
+            bool const by_seed = sm.time[i - 1] == 0.f || sm.time[i + 1] == 0.f || sm.time[i - BW] == 0.f ||
+                                 sm.time[i + BW] == 0.f;
+            open[k] = v[k] && (full || on_edge || by_seed);
+        }
+        bool any_open = false;
+#pragma unroll
+        for (int k = 0; k < G::CPT; ++k) any_open |= open[k];
+        if (__syncthreads_or(any_open)) {
+            for (;;) {
+#pragma unroll
+                for (int k = 0; k < G::CPT; ++k) {
+                    if (!open[k]) continue;
+                    int const i = idx[k];
+                    float const ax = fminf(sm.time[i - 1], sm.time[i + 1]);
+                    float const ay = fminf(sm.time[i - BW], sm.time[i + BW]);
+                    float const nt = godunov2(ax, ay, c[k], c2[k], t[k]);
+                    bool moved = false;
+                    if (nt < t[k]) {
+                        moved = time_diff(nt, t[k]) < -eps;
+                        t[k] = nt;
+                        sm.time[i] = nt;
+                        own_changed = true;
+                    }
+                    if (moved) continue;
+                    open[k] = false;  // converged: have the neighbours re-checked
+                    int const lx = lxs[k], ly = lys[k];
+                    if (lx > 0 && sm.cost[i - 1] < f_inf()) check[ly * B + lx - 1] = 1;
+                    if (lx + 1 < tc.sx && sm.cost[i + 1] < f_inf()) check[ly * B + lx + 1] = 1;
+                    if (ly > 0 && sm.cost[i - BW] < f_inf()) check[(ly - 1) * B + lx] = 1;
+                    if (ly + 1 < tc.sy && sm.cost[i + BW] < f_inf()) check[(ly + 1) * B + lx] = 1;
+                }
+                __syncthreads();
+                bool still_open = false;
+#pragma unroll
+                for (int k = 0; k < G::CPT; ++k) {
+                    if (!v[k]) continue;
+                    int const cell = lys[k] * B + lxs[k];
+                    if (check[cell]) {
+                        check[cell] = 0;
+                        if (!open[k]) {
+                            int const i = idx[k];
+                            float const ax = fminf(sm.time[i - 1], sm.time[i + 1]);
+                            float const ay = fminf(sm.time[i - BW], sm.time[i + BW]);
+                            float const nt = godunov2(ax, ay, c[k], c2[k], t[k]);
+                            if (nt < t[k]) {
+                                open[k] = time_diff(nt, t[k]) < -eps;
+                                t[k] = nt;
+                                sm.time[i] = nt;
+                                own_changed = true;
+                            }
+                        }
+                    }
+                    still_open |= open[k];
+                }
+                ++sweeps;
+                if (!__syncthreads_or(still_open)) break;
+                if (sweeps >= s.max_sweeps) {
+                    capped = true;
+                    break;
+                }
+            }
+        }
+    }
+
+    // Which edge rows this solve changed (bit e: the row facing neighbour e).
+    {
+        uint32_t ec = 0u;
+#pragma unroll
+        for (int k = 0; k < G::CPT; ++k) {
+            if (!inside[k] || t[k] == t0[k]) continue;
+            if (lxs[k] == 0) ec |= 1u;
+            if (lys[k] == 0) ec |= 2u;
+            if (lxs[k] == tc.sx - 1) ec |= 4u;
+            if (lys[k] == tc.sy - 1) ec |= 8u;
+        }
+        ec = __reduce_or_sync(0xffffffffu, ec);
+        if ((tid & 31) == 0 && ec) atomicOr(&s_word[4], ec);
+    }
+    // Probe the neighbours' edge rows: edge e, cell ei of that row.
+    int const e = tid / B;
+    int const ei = tid % B;
+    bool e_imp = false;
+    float e_key = f_inf();
+    int nb = -1;
+    if (tid < 4 * B) {
+        nb = neighbour_tile(I, tc.tx, tc.ty, e);
+        int const len = (e & 1) ? tc.sx : tc.sy;
+        if (nb >= 0 && ei < len) {
+            int px, py, qx, qy, fx, fy;
+            if (e == 0) { px = -1; py = ei; qx = 0; qy = ei; fx = -2; fy = ei; }
+            else if (e == 1) { px = ei; py = -1; qx = ei; qy = 0; fx = ei; fy = -2; }
+            else if (e == 2) { px = tc.sx; py = ei; qx = tc.sx - 1; qy = ei; fx = tc.sx + 1; fy = ei; }
+            else { px = ei; py = tc.sy; qx = ei; qy = tc.sy - 1; fx = ei; fy = tc.sy + 1; }
+            int const pi = si<B>(px, py);
+            float const cp = sm.cost[pi];
+            if (cp < f_inf()) {
+                float const told = sm.time[pi];
+                float const a_norm = fminf(sm.time[si<B>(qx, qy)], sm.time[si<B>(fx, fy)]);
+                float const a_lat = (e & 1) ? fminf(sm.time[pi - 1], sm.time[pi + 1])
+                                            : fminf(sm.time[pi - BW], sm.time[pi + BW]);
+                float const nt = godunov(a_norm, a_lat, cp, told);
+                if (time_diff(nt, told) < -eps) {
+                    e_imp = true;
+                    e_key = nt;
+                }
+            }
+        }
+#pragma unroll
+        for (int o = B / 2; o >= 1; o >>= 1) {
+            e_imp |= __shfl_xor_sync(0xffffffffu, static_cast<int>(e_imp), o) != 0;
+            e_key = fminf(e_key, __shfl_xor_sync(0xffffffffu, e_key, o));
+        }
+    }
+
+    // Commit the tile and its smallest time.
+    bool const tile_changed = __syncthreads_or(own_changed) != 0;
+    float lmin = f_inf();
+#pragma unroll
+    for (int k = 0; k < G::CPT; ++k) {
+        if (!inside[k]) continue;
+        lmin = fminf(lmin, t[k]);
+        if (tile_changed) I.time[static_cast<size_t>(tc.oy + lys[k]) * I.w + tc.ox + lxs[k]] = t[k];
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+    if ((tid & 31) == 0) s_red[tid >> 5] = lmin;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        float m = s_red[0];
+        for (int w = 1; w < G::THREADS / 32; ++w) m = fminf(m, s_red[w]);
+        s.tmin[tile] = m;
+        if (capped) activate(s, tile, kFull, m, nxt);
+    }
+    uint32_t const edge_changed = s_word[4];
+    if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u))
+        activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt);
+    GHCM_PROF_COUNT(s.ctl, 3, sweeps);
+    __syncthreads();
+    return true;
+}
+
+// Global residual judge, one tile per warp: re-activates every tile holding
+// a cell whose Godunov update would still lower it by more than eps. The
+// reference has no such check (src/eikonal_hcm.cpp:343, 486-488).
+template <int B>
+__device__ void residual_warp(const Sched& s, uint32_t nxt, uint32_t warp_global, uint32_t warps) {
+    int const lane = threadIdx.x & 31;
+    for (uint32_t tile = warp_global; tile < s.num_tiles; tile += warps) {
+        const Inst& I = s.insts[inst_of(s, tile)];
+        TileCoord const tc = tile_coord<B>(I, tile);
+        bool bad = false;
+        float kmin = f_inf();
+        for (int k = lane; k < B * B; k += 32) {
+            int const lx = k % B, ly = k / B;
+            if (lx >= tc.sx || ly >= tc.sy) continue;
+            int const gx = tc.ox + lx, gy = tc.oy + ly;
+            size_t const gi = static_cast<size_t>(gy) * I.w + gx;
+            float const cst = to_cost(I, __ldg(&I.in[gi]));
+            if (!(cst < f_inf())) continue;
+            float const t = __ldcg(&I.time[gi]);
+            float const xl = gx > 0 ? __ldcg(&I.time[gi - 1]) : f_inf();
+            float const xr = gx + 1 < static_cast<int>(I.w) ? __ldcg(&I.time[gi + 1]) : f_inf();
+            float const yu = gy > 0 ? __ldcg(&I.time[gi - I.w]) : f_inf();
+            float const yd = gy + 1 < static_cast<int>(I.h) ? __ldcg(&I.time[gi + I.w]) : f_inf();
+            float const nt = godunov(fminf(xl, xr), fminf(yu, yd), cst, t);
+            if (time_diff(nt, t) < -s.eps) {
+                bad = true;
+                kmin = fminf(kmin, nt);
+            }
+        }
+        if (__any_sync(0xffffffffu, bad)) {
+#pragma unroll
+            for (int o = 16; o >= 1; o >>= 1) kmin = fminf(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
+            if (lane == 0) activate(s, tile, kFull, kmin, nxt);
+        }
+    }
+}
+
+}  // namespace ghcm

@@ -153,14 +153,19 @@ def _seeds(seed_points) -> np.ndarray:
 
 
 def eikonal_hcm_cuda_ex(info: HcmSetup, field_cost: np.ndarray, seed_points, *, input_is_speed: bool = False,
-                        h: float = 1.0) -> EikonalResult:
-    """Solves with host arrays (copies in and out are part of the call)."""
+                        h: float = 1.0, out: np.ndarray | None = None) -> EikonalResult:
+    """Solves with host arrays (copies in and out are part of the call).
+    `out`, when given, is a C-contiguous float32 array of the field's shape
+    (pinned memory makes the copies faster) that receives the times."""
     f = np.ascontiguousarray(field_cost, dtype=np.float32)
     if f.ndim != 2:
         raise ValueError("field must be 2-D [y, x]")
     height, width = f.shape
     seeds = _seeds(seed_points)
-    out = np.empty_like(f)
+    if out is None:
+        out = np.empty_like(f)
+    elif out.shape != f.shape or out.dtype != np.float32 or not out.flags.c_contiguous:
+        raise ValueError("out must be a C-contiguous float32 array of the field's shape")
     st = GhcmStats()
     t0 = time.perf_counter()
     rc = _lib.load().ghcm_solve(info.handle, f.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), int(input_is_speed),

@@ -80,6 +80,7 @@ typedef struct ghcm_stats {
     uint32_t tiles;           /* tiles in the tiling */
     double   device_ms;       /* device time from device-resident input to converged field */
     double   total_ms;        /* host wall time of the call, copies included */
+    double   kernel_ms;       /* device time of the persistent solve kernel alone */
 } ghcm_stats;
 
 typedef struct ghcm_ctx ghcm_ctx;

@@ -18,6 +18,7 @@
 // Build with -ffp-contract=off so that no multiply-add is fused: the Godunov
 // update must round exactly like the reference build on every host.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdint>
@@ -203,6 +204,173 @@ std::int64_t fmm_sequential(const float* cost, Grid g, const std::uint32_t* seed
     return std::chrono::duration_cast<std::chrono::microseconds>(t1 - t0).count();
 }
 
+// ---------------------------------------------------------------------------
+// The reference gHCM solve with the systolic kernel, restated on the CPU:
+// host scheduler src/eikonal_hcm.cpp:186-482 and device kernel
+// data/eikonal_ghcm_systolic.cl:8-175 (+ data/eikonal_common.cl:46-359).
+// It reproduces the reference's schedule - stale priority keys, the dirty
+// set cleared after a wave's statuses are read (so a block dirtied while in
+// flight is not re-queued), check_border writing into the neighbour block -
+// to count block-solves and waves. Jobs of one wave, which the reference runs
+// concurrently, run here one after another; inside a job, every work-group
+// chunk is updated Jacobi-style (all lanes read, then all write), as the
+// lock-step wavefront does.
+// ---------------------------------------------------------------------------
+struct HcmCount {
+    std::uint64_t block_solves = 0;
+    std::uint64_t waves = 0;
+};
+
+HcmCount hcm_systolic(float eps, const float* cost, Grid g, const std::uint32_t* seeds, std::uint32_t n_seeds,
+                      std::uint32_t block, std::uint32_t max_jobs, std::uint32_t wg, float* out) {
+    std::vector<float> t(static_cast<size_t>(g.w * g.h), kInf);
+    for (std::uint32_t i = 0; i < n_seeds; ++i) t[g.idx(seeds[2 * i], seeds[2 * i + 1])] = 0.f;
+    std::int64_t const bx = (g.w + block - 1) / block, by = (g.h + block - 1) / block;
+    std::int64_t const nb = bx * by;
+    std::vector<float> smallest(static_cast<size_t>(nb), kInf);
+    std::vector<std::uint32_t> border_mask(static_cast<size_t>(nb), 0);
+    std::vector<std::uint8_t> dirty(static_cast<size_t>(nb), 0);
+
+    auto calc_min = [&](std::int64_t id) {  // BlockWrapper::calc_min_time
+        std::int64_t const cx = id % bx, cy = id / bx;
+        float m = smallest[id];
+        for (auto const& d : kSeedDirs) {
+            std::int64_t const x = cx + d[0], y = cy + d[1];
+            if (x >= 0 && y >= 0 && x < bx && y < by) m = std::min(m, smallest[x + y * bx]);
+        }
+        return m;
+    };
+    struct Wrapped {
+        std::int64_t id;
+        float recorded;
+        bool operator<(Wrapped const& o) const { return recorded > o.recorded; }
+    };
+    std::priority_queue<Wrapped> queue;
+    {  // seed_map: blocks of the seeds' 4-neighbours, in block-id order
+        std::vector<std::int64_t> seed_blocks;
+        for (std::uint32_t i = 0; i < n_seeds; ++i)
+            for (auto const& d : kSeedDirs) {
+                std::int64_t const x = static_cast<std::int64_t>(seeds[2 * i]) + d[0];
+                std::int64_t const y = static_cast<std::int64_t>(seeds[2 * i + 1]) + d[1];
+                if (g.inside(x, y)) seed_blocks.push_back((x / block) + (y / block) * bx);
+            }
+        std::stable_sort(seed_blocks.begin(), seed_blocks.end());
+        for (std::int64_t id : seed_blocks) {
+            if (dirty[id]) continue;
+            dirty[id] = 1;
+            smallest[id] = 0.f;
+            queue.push({id, calc_min(id)});
+        }
+    }
+
+    HcmCount cnt;
+    // one block-solve of the systolic kernel; returns border flags
+    auto run_job = [&](std::int64_t id, float& smin, bool flags[4]) {
+        std::int64_t const cx = id % bx, cy = id / bx;
+        std::int64_t const ox = cx * block, oy = cy * block;
+        std::int64_t const sx = std::min<std::int64_t>(block, g.w - ox), sy = std::min<std::int64_t>(block, g.h - oy);
+        std::vector<float> cache(static_cast<size_t>(sx * sy));
+        for (std::int64_t y = 0; y < sy; ++y)
+            for (std::int64_t x = 0; x < sx; ++x) cache[x + y * sx] = t[g.idx(ox + x, oy + y)];
+        // local read: tile from the cache, the one-cell ring from the global
+        // field, beyond it +inf (in_bounds_padded, data/eikonal_common.cl:199-206)
+        auto rd = [&](std::int64_t lx, std::int64_t ly) -> float {
+            if (lx < -1 || ly < -1 || lx > sx || ly > sy) return kInf;
+            if (lx >= 0 && ly >= 0 && lx < sx && ly < sy) return cache[lx + ly * sx];
+            std::int64_t const x = ox + lx, y = oy + ly;
+            return g.inside(x, y) ? t[g.idx(x, y)] : kInf;
+        };
+        auto cost_at = [&](std::int64_t lx, std::int64_t ly) {
+            std::int64_t const x = ox + lx, y = oy + ly;
+            return g.inside(x, y) ? cost[g.idx(x, y)] : 0.f;  // field_get_cost(info, 0.f, ...)
+        };
+        auto update = [&](std::int64_t lx, std::int64_t ly) {
+            float const ax = std::min(rd(lx - 1, ly), rd(lx + 1, ly));
+            float const ay = std::min(rd(lx, ly - 1), rd(lx, ly + 1));
+            return godunov_dev(std::min(ax, ay), std::max(ax, ay), cost_at(lx, ly), rd(lx, ly));
+        };
+        smin = kInf;
+        std::int64_t const len = sx * sy;
+        std::vector<float> nw(static_cast<size_t>(wg));
+        for (;;) {
+            bool converged = true;
+            for (std::int64_t base = 0; base < len; base += wg) {
+                std::int64_t const end = std::min<std::int64_t>(len, base + wg);
+                for (std::int64_t i = base; i < end; ++i) nw[i - base] = update(i % sx, i / sx);
+                for (std::int64_t i = base; i < end; ++i) {
+                    float const old = cache[i];
+                    float const v = nw[i - base];
+                    cache[i] = v;
+                    smin = std::min(smin, v);
+                    float const diff = (v == old) ? 0.f : v - old;
+                    converged &= -eps < diff;
+                }
+            }
+            if (converged) break;
+        }
+        // check_border: solve the neighbour's edge row and store if better
+        for (int e = 0; e < 4; ++e) {
+            flags[e] = false;
+            std::int64_t const nx = cx + (e == 0 ? -1 : e == 2 ? 1 : 0), ny = cy + (e == 1 ? -1 : e == 3 ? 1 : 0);
+            if (nx < 0 || ny < 0 || nx >= bx || ny >= by) continue;
+            std::int64_t const blen = (e == 0 || e == 2) ? sy : sx;
+            std::vector<float> vals(static_cast<size_t>(blen));
+            std::vector<std::int64_t> px(static_cast<size_t>(blen)), py(static_cast<size_t>(blen));
+            for (std::int64_t i = 0; i < blen; ++i) {
+                px[i] = e == 0 ? -1 : e == 2 ? sx : i;
+                py[i] = e == 1 ? -1 : e == 3 ? sy : i;
+                vals[i] = update(px[i], py[i]);
+            }
+            for (std::int64_t i = 0; i < blen; ++i) {
+                float const old = rd(px[i], py[i]);
+                t[g.idx(ox + px[i], oy + py[i])] = vals[i];
+                smin = std::min(smin, vals[i]);
+                float const diff = (vals[i] == old) ? 0.f : vals[i] - old;
+                flags[e] = flags[e] || diff <= -eps;
+            }
+        }
+        for (std::int64_t y = 0; y < sy; ++y)
+            for (std::int64_t x = 0; x < sx; ++x) t[g.idx(ox + x, oy + y)] = cache[x + y * sx];
+    };
+
+    std::vector<std::int64_t> jobs;
+    while (!queue.empty()) {
+        jobs.clear();
+        while (jobs.size() < max_jobs && !queue.empty()) {
+            jobs.push_back(queue.top().id);
+            border_mask[queue.top().id] = 0;
+            queue.pop();
+        }
+        cnt.waves += 1;
+        std::vector<std::pair<float, std::array<bool, 4>>> status(jobs.size());
+        for (size_t j = 0; j < jobs.size(); ++j) {
+            bool f[4];
+            run_job(jobs[j], status[j].first, f);
+            for (int e = 0; e < 4; ++e) status[j].second[e] = f[e];
+        }
+        cnt.block_solves += jobs.size();
+        for (size_t j = 0; j < jobs.size(); ++j) {
+            std::int64_t const id = jobs[j];
+            smallest[id] = status[j].first;
+            std::int64_t const cx = id % bx, cy = id / bx;
+            for (int e = 0; e < 4; ++e) {
+                // k_border_directions order: -x, -y, +x, +y
+                std::int64_t const x = cx + kSeedDirs[e][0], y = cy + kSeedDirs[e][1];
+                if (!status[j].second[e] || x < 0 || y < 0 || x >= bx || y >= by) continue;
+                std::int64_t const nid = x + y * bx;
+                if (!dirty[nid]) {
+                    dirty[nid] = 1;
+                    queue.push({nid, calc_min(nid)});
+                }
+                border_mask[nid] |= 1u << (8 * ((e + 2) & 3));
+            }
+        }
+        for (std::int64_t id : jobs) dirty[id] = 0;
+    }
+    std::memcpy(out, t.data(), t.size() * sizeof(float));
+    return cnt;
+}
+
 bool valid_seeds(Grid g, const std::uint32_t* seeds, std::uint32_t n) {
     if (n && !seeds) return false;
     for (std::uint32_t i = 0; i < n; ++i)
@@ -265,6 +433,21 @@ double ghcm_oracle_residual(const float* cost, const float* time, std::uint32_t 
             worst = std::max(worst, r);
         }
     return worst;
+}
+
+// The reference's gHCM schedule with the systolic kernel (see hcm_systolic):
+// arrival times into time_out, block-solve and wave counts into counts[0..1].
+int ghcm_oracle_hcm(float eps, const float* cost, std::uint32_t w, std::uint32_t h, const std::uint32_t* seeds_xy,
+                    std::uint32_t n_seeds, std::uint32_t block, std::uint32_t max_jobs, std::uint32_t wg,
+                    float* time_out, std::uint64_t* counts) {
+    Grid const g{w, h};
+    if (!cost || !time_out || !counts || w == 0 || h == 0 || block == 0 || max_jobs == 0 || wg == 0 ||
+        !valid_seeds(g, seeds_xy, n_seeds))
+        return -1;
+    HcmCount const c = hcm_systolic(eps, cost, g, seeds_xy, n_seeds, block, max_jobs, wg, time_out);
+    counts[0] = c.block_solves;
+    counts[1] = c.waves;
+    return 0;
 }
 
 // Runs `count` independent FMM (kind 0) or FIM (kind 1) solves of the same

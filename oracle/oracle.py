@@ -98,6 +98,22 @@ class Oracle(_Lib):
         t.argtypes = [ctypes.c_int, ctypes.c_float, _f32p, ctypes.c_uint32, ctypes.c_uint32, _u32p, ctypes.c_uint32,
                       ctypes.c_uint32, ctypes.c_uint32, _f32p]
         t.restype = ctypes.c_int64
+        hc = self.lib.ghcm_oracle_hcm
+        hc.argtypes = [ctypes.c_float, _f32p, ctypes.c_uint32, ctypes.c_uint32, _u32p, ctypes.c_uint32, ctypes.c_uint32,
+                       ctypes.c_uint32, ctypes.c_uint32, _f32p, ctypes.POINTER(ctypes.c_uint64)]
+        hc.restype = ctypes.c_int
+
+    def hcm(self, cost, seeds, block: int = 8, max_jobs: int = 64, eps: float = 1e-5, wg: int = 64):
+        """The reference gHCM schedule with its systolic kernel, on the CPU:
+        returns (field, block_solves, waves)."""
+        cost, seeds, w, h = _prep(cost, seeds)
+        out = np.empty((h, w), dtype=np.float32)
+        counts = (ctypes.c_uint64 * 2)()
+        rc = self.lib.ghcm_oracle_hcm(eps, _ptr(cost, _f32p), w, h, _ptr(seeds, _u32p), len(seeds), block, max_jobs,
+                                      wg, _ptr(out, _f32p), counts)
+        if rc != 0:
+            raise ValueError("hcm failed")
+        return out, int(counts[0]), int(counts[1])
 
     def fmm64(self, cost, seeds):
         """FMM carried out in FP64: the accuracy oracle."""

@@ -96,3 +96,25 @@ def test_rel_diff_conventions():
     assert rel_diff(np.array([inf, 1.0]), np.array([inf, 1.0])) == 0.0
     assert rel_diff(np.array([1.0, 2.0]), np.array([inf, 2.0])) == float("inf")
     assert abs(rel_diff(np.array([0.0, 2.0 + 2e-6]), np.array([0.0, 2.0])) - 1e-6) < 1e-9
+
+
+def test_reference_schedule_restatement_counts(oracle_lib):
+    """The CPU restatement of the reference gHCM schedule (systolic kernel)
+    runs to an empty queue and counts its block-solves and waves; on a
+    constant field nothing can be lost, so it matches FIM."""
+    g = load_golden("constant_33x17")
+    out, solves, waves = oracle_lib.hcm(g["cost"], g["seeds"], block=8, max_jobs=4)
+    assert solves >= 15 and waves >= 4  # 5 x 3 blocks, each solved at least once
+    assert rel_diff(out, g["fim_1e5"]) < 1e-5
+
+
+def test_reference_schedule_loses_wakeups_on_rings(oracle_lib):
+    """The reference schedule clears the dirty bit of every job of a wave after
+    reading the wave's statuses (src/eikonal_hcm.cpp:468-469), so a block
+    dirtied by a neighbour solved in the same wave is never re-queued: on the
+    ring field the result is not a fixed point. The device scheduler re-queues
+    such blocks and ends with a global residual check."""
+    g = load_golden("multi_seed_50")
+    out, solves, waves = oracle_lib.hcm(g["cost"], g["seeds"], block=8, max_jobs=16)
+    assert solves > 0 and waves > 0
+    assert oracle_lib.residual(g["cost"], out) > 1e-3
