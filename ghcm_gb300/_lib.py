@@ -15,6 +15,8 @@ GHCM_ERR_TIMEOUT = -5
 GHCM_ERR_NOT_CONVERGED = -6
 GHCM_ERR_UNSUPPORTED = -7
 GHCM_ERR_INTERNAL = -8
+GHCM_ERR_TOO_LARGE = -9
+GHCM_NOALLOC_MAX_TILES = 262144
 
 GHCM_KERNEL_SYSTOLIC = 0
 GHCM_KERNEL_FIM = 1
@@ -34,6 +36,7 @@ EXPORTS = (
     "ghcm_status_string",
     "ghcm_abi_version",
     "ghcm_selftest_wait_timeout",
+    "ghcm_solve_device_noalloc",
 )
 
 
@@ -107,6 +110,8 @@ def load(path: Path | None = None):
     lib.ghcm_status_string.restype = ctypes.c_char_p
     lib.ghcm_abi_version.argtypes = []
     lib.ghcm_selftest_wait_timeout.argtypes = [vp, ctypes.c_uint32]
+    lib.ghcm_solve_device_noalloc.argtypes = [cfgp, vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
+                                              vp, ctypes.c_uint32, vp, vp]
     for name in EXPORTS:
         if name != "ghcm_status_string":
             getattr(lib, name).restype = ctypes.c_int

@@ -22,9 +22,6 @@ namespace {
 using namespace ghcm;
 
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 struct DevBuf {
     void* p = nullptr;
@@ -55,6 +52,50 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 }  // namespace
 
+namespace ghcm {
+
+int check_config(const ghcm_config* c) {
+    if (!c) return GHCM_ERR_BAD_ARG;
+    if (c->block_size != 8 && c->block_size != 16 && c->block_size != 32) return GHCM_ERR_BAD_ARG;
+    if (c->kernel > GHCM_KERNEL_FIM || c->schedule > GHCM_SCHEDULE_LEARNED || c->key_mode > GHCM_KEY_BLOCK_MIN)
+        return GHCM_ERR_BAD_ARG;
+    if (!(c->eps >= 0.f) || !std::isfinite(c->eps)) return GHCM_ERR_BAD_ARG;
+    for (uint32_t r : c->reserved)
+        if (r != 0) return GHCM_ERR_BAD_ARG;
+    return GHCM_OK;
+}
+
+EncodeTiledFn tensor_map_encoder() {
+    static EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            return reinterpret_cast<EncodeTiledFn>(p);
+        cudaGetLastError();
+        return static_cast<EncodeTiledFn>(nullptr);
+    }();
+    return fn;
+}
+
+bool encode_tile_map(EncodeTiledFn encode, CUtensorMap* map, const float* base, uint32_t w, uint32_t h,
+                     uint32_t block) {
+    if (!encode) return false;
+    cuuint64_t const dims[2] = {w, h};
+    cuuint64_t const strides[1] = {static_cast<cuuint64_t>(w) * sizeof(float)};
+    uint32_t bw = 0, bh = 0;
+    tile_box(static_cast<int>(block), &bw, &bh);  // the tile with its halo, x from ox-4 (16-byte aligned)
+    cuuint32_t const box[2] = {bw, bh};
+    cuuint32_t const estr[2] = {1, 1};
+    CUresult const r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+}  // namespace ghcm
+
 struct ghcm_ctx {
     ghcm_config cfg;
     int device = 0;
@@ -79,17 +120,6 @@ int map_cuda(cudaError_t e) {
     return GHCM_ERR_CUDA;
 }
 
-int check_config(const ghcm_config* c) {
-    if (!c) return GHCM_ERR_BAD_ARG;
-    if (c->block_size != 8 && c->block_size != 16 && c->block_size != 32) return GHCM_ERR_BAD_ARG;
-    if (c->kernel > GHCM_KERNEL_FIM || c->schedule > GHCM_SCHEDULE_LEARNED || c->key_mode > GHCM_KEY_BLOCK_MIN)
-        return GHCM_ERR_BAD_ARG;
-    if (!(c->eps >= 0.f) || !std::isfinite(c->eps)) return GHCM_ERR_BAD_ARG;
-    for (uint32_t r : c->reserved)
-        if (r != 0) return GHCM_ERR_BAD_ARG;
-    return GHCM_OK;
-}
-
 struct Layout {
     size_t flags, key, tmin, list0, list1, jobs, ctl, insts, total;
 };
@@ -112,19 +142,6 @@ Layout layout_for(uint32_t tiles, uint32_t jobs) {
     l.insts = take(sizeof(Inst));
     l.total = o;
     return l;
-}
-
-bool encode_map(ghcm_ctx* ctx, CUtensorMap* map, const float* base, uint32_t w, uint32_t h, uint32_t block) {
-    cuuint64_t const dims[2] = {w, h};
-    cuuint64_t const strides[1] = {static_cast<cuuint64_t>(w) * sizeof(float)};
-    uint32_t bw = 0, bh = 0;
-    tile_box(static_cast<int>(block), &bw, &bh);  // the tile with its halo, x from ox-4 (16-byte aligned)
-    cuuint32_t const box[2] = {bw, bh};
-    cuuint32_t const estr[2] = {1, 1};
-    CUresult const r = ctx->encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
-                                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS;
 }
 
 uint32_t bytes_per_solve(uint32_t b) {
@@ -161,8 +178,8 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     bool const aligned = (w % 4u == 0u) && (reinterpret_cast<uintptr_t>(d_field) % 16u == 0u) &&
                          (reinterpret_cast<uintptr_t>(d_time) % 16u == 0u);
     I.tma = 0;
-    if (ctx->cfg.use_tma && ctx->encode && aligned && encode_map(ctx, &s.tmap_time, d_time, w, h, B) &&
-        encode_map(ctx, &s.tmap_in, d_field, w, h, B))
+    if (ctx->cfg.use_tma && aligned && encode_tile_map(ctx->encode, &s.tmap_time, d_time, w, h, B) &&
+        encode_tile_map(ctx->encode, &s.tmap_in, d_field, w, h, B))
         I.tma = 1;
 
     s.insts = reinterpret_cast<const Inst*>(base + L.insts);
@@ -255,6 +272,7 @@ const char* ghcm_status_string(int status) {
         case GHCM_ERR_NOT_CONVERGED: return "wave cap reached before convergence";
         case GHCM_ERR_UNSUPPORTED: return "unsupported device or size";
         case GHCM_ERR_INTERNAL: return "internal error";
+        case GHCM_ERR_TOO_LARGE: return "field exceeds the no-alloc scratch limit (GHCM_NOALLOC_MAX_TILES tiles)";
         default: return "unknown status";
     }
 }
@@ -305,13 +323,7 @@ int ghcm_create(const ghcm_config* cfg, ghcm_ctx** out) {
         delete ctx;
         return GHCM_ERR_UNSUPPORTED;
     }
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-        ctx->encode = reinterpret_cast<EncodeTiledFn>(fn);
-    else
-        cudaGetLastError();
+    ctx->encode = tensor_map_encoder();
     if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
         cudaEventCreate(&ctx->ev2) != cudaSuccess ||
         cudaMallocHost(reinterpret_cast<void**>(&ctx->h_inst), sizeof(Inst)) != cudaSuccess ||

@@ -6,6 +6,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include "ghcm.h"
+
 namespace ghcm {
 
 // Error bits written to Ctl::error by device code; the host maps them to
@@ -84,6 +86,16 @@ struct LaunchInfo {
     int threads;
     int blocks_per_sm;
 };
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// Host helpers implemented in ghcm_capi.cpp.
+int check_config(const ghcm_config* c);
+EncodeTiledFn tensor_map_encoder();
+bool encode_tile_map(EncodeTiledFn encode, CUtensorMap* map, const float* base, uint32_t w, uint32_t h,
+                     uint32_t block);
 
 // Host entry points implemented in ghcm_solver.cu.
 int query_persistent(int block, int fim, LaunchInfo* info);

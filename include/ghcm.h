@@ -40,6 +40,7 @@ extern "C" {
 #define GHCM_ERR_NOT_CONVERGED -6  /* the wave cap was reached before convergence */
 #define GHCM_ERR_UNSUPPORTED   -7  /* no usable GPU, or a size the build does not support */
 #define GHCM_ERR_INTERNAL      -8  /* an internal invariant failed (a bug) */
+#define GHCM_ERR_TOO_LARGE     -9  /* the field needs more tiles than ghcm_solve_device_noalloc's scratch holds */
 
 /* ghcm_config.kernel - the tile solver (HcmConfig::Kernel, src/eikonal.h:13) */
 #define GHCM_KERNEL_SYSTOLIC 0     /* sweep every cell until the tile converges */
@@ -121,6 +122,28 @@ const char* ghcm_status_string(int status);
 
 /* ABI version (GHCM_ABI_VERSION). */
 int ghcm_abi_version(void);
+
+/* Largest tiling (tiles of cfg->block_size) ghcm_solve_device_noalloc accepts:
+ * 4096 x 4096 cells at block 8, 8192 x 8192 at block 16. */
+#define GHCM_NOALLOC_MAX_TILES 262144u
+
+/* ghcm_solve_device without a context and without allocating: no cudaMalloc,
+ * cudaFree, pinned or library allocation of any kind. It has no counterpart in
+ * the reference. For callers that cannot allocate GPU memory themselves or let
+ * a library do it - a host whose pool owns every device allocation, a path that
+ * must not synchronise the device the way cudaMalloc/cudaFree can, a service
+ * whose footprint must not grow after start-up. The scheduler's scratch is one
+ * static device array of about 6 MiB that every GPU loading the library holds
+ * until exit; fields whose tiling exceeds GHCM_NOALLOC_MAX_TILES are rejected
+ * with GHCM_ERR_TOO_LARGE. Runs on the current device (cfg->device must be -1
+ * or that device) on `stream` and returns when the solve has finished.
+ * All calls share the one scratch array: calls that overlap on the GPU (other
+ * streams or host threads) race and must be serialised by the caller. The
+ * first call on a device looks up the array's device address; make it before
+ * capturing a stream into a CUDA graph. No statistics are returned. */
+int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_field, int input_is_speed, uint32_t width,
+                              uint32_t height, float h, const uint32_t* d_seeds_xy, uint32_t n_seeds,
+                              float* d_time_out, void* stream);
 
 /* Self-test of the bounded-wait path: launches a kernel that waits on a flag
  * nothing sets, with a limit of timeout_ms, and returns its status

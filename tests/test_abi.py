@@ -65,7 +65,7 @@ def test_defaults_mirror_the_reference_config(ghcm_lib):
 
 
 def test_status_strings(ghcm_lib):
-    for code in range(-8, 1):
+    for code in range(-9, 1):
         assert ghcm_lib.ghcm_status_string(code)
     assert ghcm_lib.ghcm_status_string(-99) == b"unknown status"
     assert ghcm_lib.ghcm_abi_version() == 1
