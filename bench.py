@@ -5,7 +5,8 @@
 Workload (one "step" = one solve to convergence): the 4096 x 4096 seven-ring
 speed field (radii 256..1920, barrier width 16, speed 0.01, 64-cell gaps at
 seeded angles, one centre source, h = 1), tiles of 16 x 16, device top-n
-selection with n = 1024, eps = 1e-5. Synthetic, seeded input: the reference's
+selection with n = 256 (the fastest of the configuration's n in {256, 1024,
+4096}; the other two are timed and reported beside it), eps = 1e-5. Synthetic, seeded input: the reference's
 ring images are replaced by the same construction drawn procedurally.
 
 Metric: Mcell/s to convergence = W*H / (time from device-resident speed and
@@ -40,7 +41,8 @@ METRIC = "Mcell/s to convergence (plain device top-n schedule), 1 GB300, max rel
 UNIT = "Mcell/s"
 WORKLOAD = "ring7_4096x4096"
 BLOCK = 16
-N_JOBS = 1024
+N_JOBS = 256
+N_SWEEP = (256, 1024, 4096)
 EPS = 1e-5
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB of L2
 
@@ -192,6 +194,7 @@ def main() -> int:
     ap.add_argument("--n", type=int, default=N_JOBS)
     ap.add_argument("--kernel", default="systolic", choices=["systolic", "fim"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-n-sweep", action="store_true", help="time only the headline n")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
@@ -253,6 +256,35 @@ def main() -> int:
         ms = float(t.item())
     value = world * cells / (ms * 1e3)
 
+    # the configuration's other n values, timed the same way (device-resident)
+    n_sweep = {}
+    if not args.no_n_sweep:
+        for n in N_SWEEP:
+            if n == args.n:
+                n_sweep[str(n)] = {"mcells": cells / (ms * 1e3), "ms": ms,
+                                   "block_solves": statistics.mean(st["block_solves"] for st in stats),
+                                   "waves": statistics.mean(st["waves"] for st in stats)}
+                continue
+            other = g.HcmSetup(g.HcmConfig(block_size=args.block, max_jobs=n, fim_minimum_change=EPS,
+                                           kernel=cfg.kernel))
+            for _ in range(args.warmup):
+                g.solve_device(other, d_speed, d_seeds, d_time, stream=stream)
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(args.steps)]
+            sts = []
+            for i in range(args.steps):
+                flush.fill_(float(i))
+                evs[i][0].record(stream)
+                sts.append(g.solve_device(other, d_speed, d_seeds, d_time, stream=stream))
+                evs[i][1].record(stream)
+            torch.cuda.synchronize(dev)
+            n_ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+            n_sweep[str(n)] = {"mcells": cells / (n_ms * 1e3), "ms": n_ms,
+                               "block_solves": statistics.mean(x["block_solves"] for x in sts),
+                               "waves": statistics.mean(x["waves"] for x in sts)}
+            other.close()
+        g.solve_device(setup, d_speed, d_seeds, d_time, stream=stream)  # leave the headline field in d_time
+
     # end to end through the host-pointer call: pinned speed in, time field out
     h_speed = torch.from_numpy(speed).pin_memory()
     h_time = torch.empty((h, w), dtype=torch.float32).pin_memory()
@@ -284,9 +316,10 @@ def main() -> int:
         "e2e": {"value": world * cells / (e2e_mean * 1e3), "unit": UNIT, "ms_per_step": e2e_mean,
                 "h2d_bytes_per_step": cells * 4 + int(seeds.nbytes), "d2h_bytes_per_step": cells * 4},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": load_traffic(), "kernel": "k_solve<16,systolic>",
+                     "traffic": load_traffic(), "kernel": f"k_solve<{args.block},{args.kernel}>",
                      "bytes_per_block_solve": bps, "block_solves": solves, "kernel_ms": k_ms,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in peaks else "fallback"},
+        "n_sweep": n_sweep,
         "gpu_launches": 5 * args.steps,
         "clocks": clocks,
         "solver": {"waves": statistics.mean(st["waves"] for st in stats),

@@ -219,10 +219,12 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     Ctl const& c = *ctx->h_ctl;
 #ifdef GHCM_PROFILE
     std::fprintf(stderr,
-                 "[ghcm-prof] grid %d solves %llu waves %u residual_passes %u barrier_ns %llu solve_ns %llu sweeps %llu "
-                 "residual_ns %llu kernel_ns %llu\n",
-                 grid, c.block_solves, c.waves, c.residual_passes, c.prof[0], c.prof[1], c.prof[3], c.prof[4],
-                 c.prof[5]);
+                 "[ghcm-prof] grid %d solves %llu waves %u residual_passes %u kernel_us %.1f | per wave: "
+                 "decide %.2f us, span %.2f us, release seen after %.2f us, max sweeps %.1f | sweeps/solve %.1f\n",
+                 grid, c.block_solves, c.waves, c.residual_passes, c.prof[5] / 1e3,
+                 c.prof[2] / 1e3 / std::max(1ull, c.prof[9]), c.prof[6] / 1e3 / std::max(1ull, c.prof[9]),
+                 c.prof[7] / 1e3 / std::max(1ull, c.prof[9]) / std::max(1, grid - 1),
+                 double(c.prof[8]) / std::max(1ull, c.prof[9]), double(c.prof[3]) / std::max(1ull, c.block_solves));
 #endif
     if (stats) {
         float ms = 0.f, kms = 0.f;

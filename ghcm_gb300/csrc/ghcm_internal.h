@@ -43,18 +43,17 @@ struct Inst {
 
 // Device-side control block of one solve.
 struct Ctl {
-    uint32_t bar_count, bar_gen;   // grid barrier words (BarrierWords layout)
+    unsigned long long release;    // wave-barrier release word: generation + the decided phase
+    uint32_t bar_count;            // CTAs arrived at the current wave barrier
     uint32_t error;                // kErr* bits
-    uint32_t phase;                // scheduler phase (kPhase*)
-    uint32_t cur;                  // list the current jobs come from; activations go to list[cur ^ 1]
     uint32_t count[2];             // sizes of the two active lists
-    uint32_t job_count;            // jobs selected for the current wave
-    uint32_t jobs_in_list;         // 1: jobs are list[cur] itself; 0: the jobs array
     uint32_t waves;
     uint32_t residual_passes;
     uint32_t max_active;
     unsigned long long block_solves;
-    unsigned long long prof[8];    // GHCM_PROFILE builds: per-phase nanoseconds and sweep counts
+    unsigned long long prof[16];   // GHCM_PROFILE builds: per-phase nanoseconds and sweep counts
+    unsigned long long release_ns; // GHCM_PROFILE builds: when the last barrier was released
+    uint32_t wave_max_sweeps;      // GHCM_PROFILE builds: most sweeps of one block-solve in this wave
 };
 
 // Everything the persistent kernel needs; passed by value as a

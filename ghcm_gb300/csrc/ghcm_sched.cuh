@@ -1,5 +1,5 @@
 // Device-side block scheduler: tile addressing, neighbour activation, the
-// top-n radix select and the wave barrier whose last arriving CTA decides the
+// top-n histogram select and the wave barrier whose last arriving CTA decides the
 // next phase. Replaces the host priority queue and activation loop of
 // src/eikonal_hcm.cpp:343-469.
 #pragma once
@@ -81,71 +81,99 @@ __device__ __forceinline__ uint32_t tile_key(const Sched& s, uint32_t tile) {
     return __float_as_uint(k);
 }
 
-// Radix select of the `n` smallest keys among the m tiles of `list`, by the
-// whole CTA: selected tiles go to s.jobs, the rest to `carry`. Keys are
-// non-negative floats, so their bit patterns order like their values.
-// Returns the number of carried tiles.
+// Selects the n smallest keys among the m (> n) tiles of `list`, by the whole
+// CTA: a histogram of SELECT_BINS bins over [min key, max key], a scan for the
+// bin holding the n-th key, then every tile of a lower bin and enough tiles of
+// that bin (in list order) go to s.jobs, the rest to `carry`. The order is
+// exact up to 1/SELECT_BINS of the key range. Returns the number carried.
+constexpr int SELECT_BINS = 2048;
+
 template <int THREADS>
 __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t m, uint32_t n, uint32_t* carry,
                                  uint32_t* s_hist, uint32_t* s_sel) {
+    __shared__ float s_fmin[THREADS / 32], s_fmax[THREADS / 32];
     int const tid = threadIdx.x;
-    uint32_t prefix = 0u, pmask = 0u, rank = n;
-    for (int shift = 24; shift >= 0; shift -= 8) {
-        for (int i = tid; i < 256; i += THREADS) s_hist[i] = 0u;
-        __syncthreads();
-        for (uint32_t i = tid; i < m; i += THREADS) {
-            uint32_t const k = tile_key(s, __ldcg(&list[i]));
-            if ((k & pmask) == prefix) atomicAdd(&s_hist[(k >> shift) & 255u], 1u);
+    int const lane = tid & 31, warp = tid >> 5;
+    // pass 1: range of the finite keys
+    float lo = f_inf(), hi = 0.f;
+    for (uint32_t i = tid; i < m; i += THREADS) {
+        float const k = __uint_as_float(tile_key(s, __ldcg(&list[i])));
+        if (k < f_inf()) {
+            lo = fminf(lo, k);
+            hi = fmaxf(hi, k);
         }
-        __syncthreads();
-        if (tid < 32) {
-            uint32_t part[8];
-            uint32_t tot = 0u;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                part[j] = s_hist[tid * 8 + j];
-                tot += part[j];
-            }
-            uint32_t incl = tot;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t const v = __shfl_up_sync(0xffffffffu, incl, o);
-                if (tid >= o) incl += v;
-            }
-            uint32_t below = incl - tot;
-            if (below < rank && rank <= incl) {
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    if (below + part[j] >= rank) {
-                        s_sel[0] = static_cast<uint32_t>(tid * 8 + j);
-                        s_sel[1] = below;
-                        break;
-                    }
-                    below += part[j];
-                }
-            }
-        }
-        __syncthreads();
-        rank -= s_sel[1];
-        prefix |= s_sel[0] << shift;
-        pmask |= 255u << shift;
-        // every key equal to the prefix so far is taken: no need to refine
-        if (s_hist[s_sel[0]] == rank) break;
-        __syncthreads();
     }
-    // take every key below the boundary prefix and `rank` keys that match it
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if (lane == 0) {
+        s_fmin[warp] = lo;
+        s_fmax[warp] = hi;
+    }
+    for (int i = tid; i < SELECT_BINS; i += THREADS) s_hist[i] = 0u;
     __syncthreads();
+    lo = s_fmin[0];
+    hi = s_fmax[0];
+    for (int w = 1; w < THREADS / 32; ++w) {
+        lo = fminf(lo, s_fmin[w]);
+        hi = fmaxf(hi, s_fmax[w]);
+    }
+    float const span = hi - lo;
+    float const scale = (span > 0.f) ? static_cast<float>(SELECT_BINS - 1) / span : 0.f;
+    auto bin_of = [&](float k) -> int {
+        if (!(k < f_inf())) return SELECT_BINS - 1;
+        int const b = static_cast<int>((k - lo) * scale);
+        return b < 0 ? 0 : (b >= SELECT_BINS ? SELECT_BINS - 1 : b);
+    };
+    // pass 2: histogram
+    for (uint32_t i = tid; i < m; i += THREADS)
+        atomicAdd(&s_hist[bin_of(__uint_as_float(tile_key(s, __ldcg(&list[i]))))], 1u);
+    __syncthreads();
+    // the bin holding the n-th smallest key: thread t scans bins [t*PER, (t+1)*PER)
+    constexpr int PER = SELECT_BINS / THREADS;
+    uint32_t part = 0u;
+#pragma unroll
+    for (int j = 0; j < PER; ++j) part += s_hist[tid * PER + j];
+    uint32_t incl = part;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t const v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    __shared__ uint32_t s_wsum[THREADS / 32];
+    if (lane == 31) s_wsum[warp] = incl;
+    __syncthreads();
+    uint32_t wbase = 0u;
+    for (int w = 0; w < warp; ++w) wbase += s_wsum[w];
+    uint32_t below = wbase + incl - part;
+    if (below < n && n <= below + part) {
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            uint32_t const h = s_hist[tid * PER + j];
+            if (below + h >= n) {
+                s_sel[0] = static_cast<uint32_t>(tid * PER + j);
+                s_sel[1] = n - below;  // how many of the boundary bin to take
+                break;
+            }
+            below += h;
+        }
+    }
     if (tid == 0) {
         s_sel[2] = 0u;
         s_sel[3] = 0u;
         s_sel[4] = 0u;
     }
     __syncthreads();
+    int const bnd = static_cast<int>(s_sel[0]);
+    uint32_t const take_eq = s_sel[1];
+    // pass 3: gather
     for (uint32_t i = tid; i < m; i += THREADS) {
         uint32_t const t = __ldcg(&list[i]);
-        uint32_t const k = tile_key(s, t);
-        bool take = (k & pmask) < prefix;
-        if (!take && (k & pmask) == prefix) take = atomicAdd(&s_sel[2], 1u) < rank;
+        int const b = bin_of(__uint_as_float(tile_key(s, t)));
+        bool take = b < bnd;
+        if (!take && b == bnd) take = atomicAdd(&s_sel[2], 1u) < take_eq;
         if (take)
             s.jobs[atomicAdd(&s_sel[3], 1u)] = t;
         else
@@ -155,104 +183,164 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
     return s_sel[4];
 }
 
+// The scheduler state each CTA keeps in shared memory (s_state[]), refreshed
+// from the release word at every wave barrier.
+enum : int { kStPhase = 0, kStCur = 1, kStJobs = 2, kStInList = 3, kStError = 4, kStWaves = 5, kStGen = 6 };
+
+// Release word: the decision of the last CTA, published with the release.
+//   bits 0-31 job count, 32-35 phase, 36 cur, 37 jobs-in-list, 38 error,
+//   40-63 barrier generation.
+__device__ __forceinline__ unsigned long long pack_release(uint32_t gen, uint32_t phase, uint32_t cur, uint32_t jobs,
+                                                           uint32_t in_list, uint32_t err) {
+    return static_cast<unsigned long long>(jobs) | (static_cast<unsigned long long>(phase & 15u) << 32) |
+           (static_cast<unsigned long long>(cur & 1u) << 36) | (static_cast<unsigned long long>(in_list & 1u) << 37) |
+           (static_cast<unsigned long long>(err ? 1u : 0u) << 38) |
+           (static_cast<unsigned long long>(gen & 0xffffffu) << 40);
+}
+
+__device__ __forceinline__ void unpack_release(unsigned long long w, uint32_t* st) {
+    uint32_t const phase = static_cast<uint32_t>(w >> 32) & 15u;
+    st[kStJobs] = static_cast<uint32_t>(w);
+    st[kStPhase] = phase;
+    st[kStCur] = static_cast<uint32_t>(w >> 36) & 1u;
+    st[kStInList] = static_cast<uint32_t>(w >> 37) & 1u;
+    st[kStError] = static_cast<uint32_t>(w >> 38) & 1u;
+    st[kStGen] = static_cast<uint32_t>(w >> 40) & 0xffffffu;
+    if (phase == kPhaseJobs) st[kStWaves] += 1u;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 // Decides the next phase; run by the whole of the last CTA to reach the wave
-// barrier while every other CTA waits.
+// barrier while every other CTA waits. `st` is this CTA's view of the state
+// the previous barrier published. Returns the new
+// {jobs-in-list, phase, cur, job count} in s_sel[8..11].
 //   after INIT / JOBS / RESIDUAL, the set to process is list[act]:
 //     non-empty          -> JOBS on its n lowest keys (the rest carried over)
 //     empty after JOBS   -> RESIDUAL: the global fixed-point check
 //     empty after RESID. -> DONE
 template <int THREADS>
-__device__ void decide_phase(const Sched& s, uint32_t* s_hist, uint32_t* s_sel) {
+__device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_hist, uint32_t* s_sel) {
     Ctl* ctl = s.ctl;
     int const tid = threadIdx.x;
-    uint32_t const prev = ld_relaxed(&ctl->phase);
-    uint32_t const cur = ld_relaxed(&ctl->cur);
+    uint32_t const prev = st[kStPhase];
+    uint32_t const cur = st[kStCur];
     uint32_t const act = (prev == kPhaseInit) ? 0u : (cur ^ 1u);
     uint32_t const m = ld_relaxed(&ctl->count[act]);
+    uint32_t phase, ncur = cur, jobs = 0u, in_list = 0u;
     if (m == 0u) {
-        if (tid == 0) {
-            if (prev == kPhaseResidual) {
-                ctl->phase = kPhaseDone;
-            } else {
-                ctl->phase = kPhaseResidual;
-                ctl->cur = act ^ 1u;  // residual activations go to list[act], now empty
+        if (prev == kPhaseResidual) {
+            phase = kPhaseDone;
+        } else {
+            phase = kPhaseResidual;
+            ncur = act ^ 1u;  // residual activations go to list[act], now empty
+            if (tid == 0) {
                 ctl->count[act] = 0u;
-                ctl->residual_passes += 1u;
+                atomicAdd(&ctl->residual_passes, 1u);
             }
         }
-        return;
-    }
-    if (s.max_waves != 0u && ld_relaxed(&ctl->waves) >= s.max_waves) {
+    } else if (s.max_waves != 0u && st[kStWaves] >= s.max_waves) {
+        phase = kPhaseStop;
+        if (tid == 0) atomicOr(&ctl->error, kErrNotConverged);
+    } else {
+        uint32_t carried = 0u;
+        bool const all = m <= s.max_jobs;
+        if (!all) carried = select_top_n<THREADS>(s, s.list[act], m, s.max_jobs, s.list[act ^ 1u], s_hist, s_sel);
+        phase = kPhaseJobs;
+        ncur = act;
+        jobs = all ? m : m - carried;
+        in_list = all ? 1u : 0u;
         if (tid == 0) {
-            atomicOr(&ctl->error, kErrNotConverged);
-            ctl->phase = kPhaseStop;
+            ctl->count[act ^ 1u] = carried;
+            atomicAdd(&ctl->waves, 1u);
+            atomicMax(&ctl->max_active, m);
         }
-        return;
     }
-    uint32_t carried = 0u;
-    bool const all = m <= s.max_jobs;
-    if (!all) carried = select_top_n<THREADS>(s, s.list[act], m, s.max_jobs, s.list[act ^ 1u], s_hist, s_sel);
     if (tid == 0) {
-        ctl->job_count = all ? m : m - carried;
-        ctl->jobs_in_list = all ? 1u : 0u;
-        ctl->count[act ^ 1u] = carried;
-        ctl->cur = act;
-        ctl->phase = kPhaseJobs;
-        ctl->waves += 1u;
-        if (m > ctl->max_active) ctl->max_active = m;
+        s_sel[8] = in_list;
+        s_sel[9] = phase;
+        s_sel[10] = ncur;
+        s_sel[11] = jobs;
     }
 }
 
 // Grid-wide wave barrier. Every CTA arrives; the last one to arrive decides
-// the next phase (decide_phase) before releasing the others. The waits are
-// bounded. On return, s_state holds {phase, cur, job_count, jobs_in_list};
-// returns false when the grid must stop (timeout or error).
+// the next phase (decide_phase) and releases the others with one 64-bit word
+// that carries the decision, so a released CTA needs no further load. The
+// waits are bounded. On return s_state holds the new state; returns false
+// when the grid must stop (timeout or error).
 template <int THREADS>
 __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, uint32_t* s_state) {
     __shared__ uint32_t s_last;
     Ctl* ctl = s.ctl;
-    BarrierWords* bw = reinterpret_cast<BarrierWords*>(ctl);
     __syncthreads();
-    uint32_t gen = 0u;
     if (threadIdx.x == 0) {
-        gen = ld_relaxed(&bw->gen);
-        __threadfence();
-        uint32_t const arrived = atomicAdd(&bw->count, 1u) + 1u;
-        __threadfence();
+        __threadfence();  // publish this CTA's work
+        uint32_t const arrived = atomicAdd(&ctl->bar_count, 1u) + 1u;
         s_last = (arrived == gridDim.x) ? 1u : 0u;
+        if (s_last) {
+            __threadfence();  // acquire everyone's work
+            ctl->bar_count = 0u;
+        }
     }
     __syncthreads();
     if (s_last) {
-        if (threadIdx.x == 0) bw->count = 0u;
-        if (ld_relaxed(&ctl->error) == 0u) decide_phase<THREADS>(s, s_hist, s_sel);
+#ifdef GHCM_PROFILE
+        uint64_t const t_last = global_ns();
+        if (threadIdx.x == 0) {
+            if (ctl->release_ns) ctl->prof[6] += t_last - ctl->release_ns;  // release -> last arrival
+            ctl->prof[8] += ctl->wave_max_sweeps;
+            ctl->wave_max_sweeps = 0u;
+        }
+#endif
+        decide_phase<THREADS>(s, s_state, s_hist, s_sel);
         __syncthreads();
         if (threadIdx.x == 0) {
+            uint32_t const err = ld_relaxed(&ctl->error);
+            unsigned long long const w =
+                pack_release(s_state[kStGen] + 1u, s_sel[9], s_sel[10], s_sel[11], s_sel[8], err);
+#ifdef GHCM_PROFILE
+            uint64_t const t_rel = global_ns();
+            ctl->prof[2] += t_rel - t_last;  // decide
+            ctl->prof[9] += 1u;
+            ctl->release_ns = t_rel;
+#endif
             __threadfence();
-            atomicAdd(&bw->gen, 1u);
+            st_release_u64(&ctl->release, w);
+            unpack_release(w, s_state);
         }
     } else if (threadIdx.x == 0) {
+        uint32_t const gen = s_state[kStGen];
         uint64_t const t0 = global_ns();
         uint32_t spins = 0;
-        while (ld_acquire(&bw->gen) == gen) {
+        unsigned long long w;
+        for (;;) {
+            w = ld_acquire_u64(&ctl->release);
+            if ((static_cast<uint32_t>(w >> 40) & 0xffffffu) != gen) break;
             if (++spins > 32) {
                 __nanosleep(32);
                 if (global_ns() - t0 > s.timeout_ns) {
                     atomicOr(&ctl->error, kErrTimeout);
+                    w = pack_release(gen, kPhaseStop, 0u, 0u, 0u, 1u);
                     break;
                 }
             }
         }
-    }
-    if (threadIdx.x == 0) {
-        __threadfence();
-        s_state[0] = ld_relaxed(&ctl->phase);
-        s_state[1] = ld_relaxed(&ctl->cur);
-        s_state[2] = ld_relaxed(&ctl->job_count);
-        s_state[3] = ld_relaxed(&ctl->jobs_in_list);
-        s_state[4] = ld_relaxed(&ctl->error);
+#ifdef GHCM_PROFILE
+        atomicAdd(&ctl->prof[7], static_cast<unsigned long long>(global_ns() - ld_relaxed_u64(&ctl->release_ns)));
+#endif
+        unpack_release(w, s_state);
     }
     __syncthreads();
-    return s_state[4] == 0u;
+    return s_state[kStError] == 0u;
 }
 
 }  // namespace ghcm

@@ -5,7 +5,7 @@
 //
 //   wave loop (replaces the host loop of src/eikonal_hcm.cpp:343-482)
 //     barrier  every CTA arrives; the last to arrive picks the n active tiles
-//              with the smallest keys (radix select over the float-bit keys:
+//              with the smallest keys (a histogram select over the keys:
 //              the device form of the priority-queue pop,
 //              src/eikonal_hcm.cpp:344-358) and releases the grid;
 //     solve    each CTA takes jobs in turn: stages the tile plus a two-cell
@@ -38,6 +38,7 @@
 #endif
 
 #include "ghcm_tile.cuh"
+#include "ghcm_warp_tile.cuh"
 
 #include <algorithm>
 
@@ -55,8 +56,8 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS) k_solve(const __grid_con
     using G = TileGeom<B>;
     __shared__ TileSmem<B> sm;
     __shared__ __align__(8) uint64_t s_bar;
-    __shared__ uint32_t s_hist[256];
-    __shared__ uint32_t s_sel[8];
+    __shared__ uint32_t s_hist[SELECT_BINS];
+    __shared__ uint32_t s_sel[16];
     __shared__ uint32_t s_state[8];
     __shared__ uint32_t s_word[8];
     __shared__ float s_red[G::THREADS / 32];
@@ -67,6 +68,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS) k_solve(const __grid_con
     if (tid == 0) mbar_init(&s_bar, 1);
     if (FIM)
         for (int i = tid; i < B * B; i += G::THREADS) sm.check[i] = 0;
+    if (tid < 8) s_state[tid] = 0u;  // INIT, generation 0, no waves yet
     __syncthreads();
     GHCM_PROF_BEGIN(t_kernel);
     uint32_t parity = 0u;
@@ -80,12 +82,12 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS) k_solve(const __grid_con
         bool const ok = wave_barrier<G::THREADS>(s, s_hist, s_sel, s_state);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
-        uint32_t const phase = s_state[0];
-        uint32_t const cur = s_state[1];
+        uint32_t const phase = s_state[kStPhase];
+        uint32_t const cur = s_state[kStCur];
         if (phase == kPhaseJobs) {
             GHCM_PROF_BEGIN(t_solve);
-            uint32_t const nj = s_state[2];
-            const uint32_t* jobs = s_state[3] ? s.list[cur] : s.jobs;
+            uint32_t const nj = s_state[kStJobs];
+            const uint32_t* jobs = s_state[kStInList] ? s.list[cur] : s.jobs;
             for (uint32_t j = blockIdx.x; j < nj; j += gridDim.x) {
                 if (!solve_tile<B, FIM>(s, __ldcg(&jobs[j]), cur ^ 1u, sm, &s_bar, parity, tma_pending, s_word, s_red))
                     break;
@@ -107,6 +109,61 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS) k_solve(const __grid_con
     // A TMA copy still in flight after a timed-out wait: give it a bounded
     // chance to land before the CTA's shared memory is released.
     if (tid == 0 && tma_pending) (void)mbar_wait(&s_bar, parity ^ 1u, s.timeout_ns);
+}
+
+// The same wave loop with one warp per tile (systolic, B = 8 or 16).
+template <int B>
+__global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(const __grid_constant__ Sched s) {
+    using W = WarpTileGeom<B>;
+    __shared__ WarpTileSmem<B> wsm[W::NW];
+    __shared__ uint32_t s_hist[SELECT_BINS];
+    __shared__ uint32_t s_sel[16];
+    __shared__ uint32_t s_state[8];
+    int const tid = threadIdx.x;
+    int const warp = tid >> 5;
+    int const lane = tid & 31;
+    WarpTileSmem<B>& sm = wsm[warp];
+    Ctl* ctl = s.ctl;
+    if (ld_relaxed(&ctl->error) != 0u) return;  // the init kernels rejected the input
+
+    if (lane == 0) mbar_init(&sm.bar, 1);
+    if (tid < 8) s_state[tid] = 0u;  // INIT, generation 0, no waves yet
+    __syncthreads();
+    GHCM_PROF_BEGIN(t_kernel);
+    uint32_t parity = 0u;
+    bool tma_pending = false;
+    unsigned long long solves = 0ull;
+    uint32_t const gw = blockIdx.x * W::NW + static_cast<uint32_t>(warp);
+    uint32_t const nwarps = gridDim.x * W::NW;
+    for (;;) {
+        GHCM_PROF_BEGIN(t_bar);
+        bool const ok = wave_barrier<W::THREADS>(s, s_hist, s_sel, s_state);
+        GHCM_PROF_END(ctl, 0, t_bar);
+        if (!ok) break;
+        uint32_t const phase = s_state[kStPhase];
+        uint32_t const cur = s_state[kStCur];
+        if (phase == kPhaseJobs) {
+            GHCM_PROF_BEGIN(t_solve);
+            uint32_t const nj = s_state[kStJobs];
+            const uint32_t* jobs = s_state[kStInList] ? s.list[cur] : s.jobs;
+            for (uint32_t j = gw; j < nj; j += nwarps) {
+                if (!solve_tile_warp<B>(s, __ldcg(&jobs[j]), cur ^ 1u, sm, parity, tma_pending)) break;
+                ++solves;
+            }
+            GHCM_PROF_END(ctl, 1, t_solve);
+        } else if (phase == kPhaseResidual) {
+            GHCM_PROF_BEGIN(t_res);
+            residual_warp<B>(s, cur ^ 1u, gw, nwarps);
+            GHCM_PROF_END(ctl, 4, t_res);
+        } else {
+            break;  // done or stopped
+        }
+    }
+    if (lane == 0 && solves) atomicAdd(&ctl->block_solves, solves);
+    if (blockIdx.x == 0) {
+        GHCM_PROF_END(ctl, 5, t_kernel);
+    }
+    if (lane == 0 && tma_pending) (void)mbar_wait(&sm.bar, parity ^ 1u, s.timeout_ns);
 }
 
 // ---------------------------------------------------------------------------
@@ -188,16 +245,23 @@ static void* kernel_ptr() {
     return reinterpret_cast<void*>(&k_solve<B, FIM>);
 }
 
+// Systolic B = 8 runs one warp per tile; everything else one CTA per tile (for
+// B = 16 the 8-warp CTA per tile measured 1.8x faster than a warp per tile on
+// the 4096^2 rings: a wave waits for its slowest tile, and a tile's sweeps are
+// shorter spread over 8 warps).
+static bool warp_tiles(int block, int fim) { return !fim && block == 8; }
+
 static void* select_kernel(int block, int fim) {
     switch (block) {
-        case 8: return fim ? kernel_ptr<8, true>() : kernel_ptr<8, false>();
+        case 8: return fim ? kernel_ptr<8, true>() : reinterpret_cast<void*>(&k_solve_warp<8>);
         case 16: return fim ? kernel_ptr<16, true>() : kernel_ptr<16, false>();
         case 32: return fim ? kernel_ptr<32, true>() : kernel_ptr<32, false>();
         default: return nullptr;
     }
 }
 
-static int threads_for(int block) {
+static int threads_for(int block, int fim) {
+    if (warp_tiles(block, fim)) return WarpTileGeom<8>::THREADS;
     switch (block) {
         case 8: return TileGeom<8>::THREADS;
         case 16: return TileGeom<16>::THREADS;
@@ -206,7 +270,8 @@ static int threads_for(int block) {
     }
 }
 
-static int cap_for(int block) {
+static int cap_for(int block, int fim) {
+    if (warp_tiles(block, fim)) return 4;
     switch (block) {
         case 8: return max_ctas_per_sm<8>();
         case 16: return max_ctas_per_sm<16>();
@@ -226,11 +291,11 @@ void tile_box(int block, uint32_t* width, uint32_t* height) {
 int query_persistent(int block, int fim, LaunchInfo* info) {
     void* k = select_kernel(block, fim);
     if (!k) return -1;
-    int const threads = threads_for(block);
+    int const threads = threads_for(block, fim);
     int bps = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, threads, 0) != cudaSuccess) return -3;
     info->threads = threads;
-    info->blocks_per_sm = std::min(bps, cap_for(block));
+    info->blocks_per_sm = std::min(bps, cap_for(block, fim));
     return 0;
 }
 
@@ -257,7 +322,7 @@ cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cuda
     void* k = select_kernel(block, fim);
     if (!k) return cudaErrorInvalidValue;
     void* args[] = {const_cast<Sched*>(&s)};
-    return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(threads_for(block)), args, 0, st);
+    return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(threads_for(block, fim)), args, 0, st);
 }
 
 cudaError_t launch_wait_selftest(uint32_t* flag, Ctl* ctl, uint64_t timeout_ns, cudaStream_t st) {

@@ -9,8 +9,7 @@
 //             reading its four neighbours from shared memory) until a sweep
 //             moves no cell by more than eps; the reference sweeps
 //             work-group-sized chunks the same way
-//             (data/eikonal_ghcm_systolic.cl:130-153). Rows whose neighbourhood
-//             did not change in the previous sweep are skipped.
+//             (data/eikonal_ghcm_systolic.cl:130-153).
 //   block-FIM only open cells are solved; a converged cell asks its in-tile
 //             neighbours to re-check and a neighbour that improves by more
 //             than eps opens (data/eikonal_ghcm_fim.cl:166-210, 347-372).
@@ -80,10 +79,7 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
         __threadfence();
         s_word[0] = f;
         s_word[1] = 0u;  // abort flag
-        s_word[4] = 0u;           // edge rows changed by this solve
-        s_word[5] = 0xffffffffu;  // rows changed, by sweep mod 3: sweep k reads [5 + k%3],
-        s_word[6] = 0u;           // writes [5 + (k+1)%3] and clears [5 + (k+2)%3];
-        s_word[7] = 0u;           // the first sweep evaluates every row
+        s_word[4] = 0u;  // edge rows changed by this solve
         if (use_tma) {
             fence_proxy_async();
             mbar_arrive_expect_tx(bar, static_cast<uint32_t>(2 * G::BOX * sizeof(float)));
@@ -147,15 +143,10 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
 
     if (!FIM) {
         for (;;) {
-            uint32_t const rd = sweeps % 3u;
-            uint32_t const rows = s_word[5 + rd];
             bool moved = false;
-            uint32_t my_rows = 0u;
 #pragma unroll
             for (int k = 0; k < G::CPT; ++k) {
-                int const y = lys[k];
-                uint32_t const near = (1u << y) | (y > 0 ? 1u << (y - 1) : 0u) | (y + 1 < B ? 1u << (y + 1) : 0u);
-                if (!v[k] || !(rows & near)) continue;
+                if (!v[k]) continue;
                 int const i = idx[k];
                 float const ax = fminf(sm.time[i - 1], sm.time[i + 1]);
                 float const ay = fminf(sm.time[i - BW], sm.time[i + BW]);
@@ -165,13 +156,8 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
                     t[k] = nt;
                     sm.time[i] = nt;
                     own_changed = true;
-                    my_rows |= 1u << y;
                 }
             }
-            // rows changed in this sweep: one shared atomic per warp
-            my_rows = __reduce_or_sync(0xffffffffu, my_rows);
-            if ((tid & 31) == 0 && my_rows) atomicOr(&s_word[5 + (rd + 1u) % 3u], my_rows);
-            if (tid == 0) s_word[5 + (rd + 2u) % 3u] = 0u;
             ++sweeps;
             if (!__syncthreads_or(moved)) break;
             if (sweeps >= s.max_sweeps) {
@@ -315,18 +301,30 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
     if ((tid & 31) == 0) s_red[tid >> 5] = lmin;
-    __threadfence();
     __syncthreads();
+    // an activating thread fences once: the barrier above has made every
+    // thread's tile stores visible to it, the fence orders them before its
+    // activation (cumulativity), so the neighbour's stage sees them
     if (tid == 0) {
         float m = s_red[0];
         for (int w = 1; w < G::THREADS / 32; ++w) m = fminf(m, s_red[w]);
         s.tmin[tile] = m;
-        if (capped) activate(s, tile, kFull, m, nxt);
+        if (capped) {
+            __threadfence();
+            activate(s, tile, kFull, m, nxt);
+        }
     }
     uint32_t const edge_changed = s_word[4];
-    if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u))
+    if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u)) {
+        __threadfence();
         activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt);
-    GHCM_PROF_COUNT(s.ctl, 3, sweeps);
+    }
+#ifdef GHCM_PROFILE
+    if (tid == 0) {
+        atomicAdd(&s.ctl->prof[3], static_cast<unsigned long long>(sweeps));
+        atomicMax(&s.ctl->wave_max_sweeps, sweeps);
+    }
+#endif
     __syncthreads();
     return true;
 }
