@@ -18,3 +18,11 @@ from .eikonal import (  # noqa: F401
     eikonal_hcm_cuda_setup,
     solve_device,
 )
+from .batch import (  # noqa: F401
+    Batch,
+    DeviceInstance,
+    autotune_batch,
+    shard_instances,
+    solve_batched,
+    solve_sharded,
+)

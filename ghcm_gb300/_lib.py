@@ -37,6 +37,12 @@ EXPORTS = (
     "ghcm_abi_version",
     "ghcm_selftest_wait_timeout",
     "ghcm_solve_device_noalloc",
+    "ghcm_batch_create",
+    "ghcm_batch_run",
+    "ghcm_batch_query",
+    "ghcm_batch_destroy",
+    "ghcm_solve_batched",
+    "ghcm_autotune_batch",
 )
 
 
@@ -69,6 +75,52 @@ class GhcmStats(ctypes.Structure):
         ("device_ms", ctypes.c_double),
         ("total_ms", ctypes.c_double),
         ("kernel_ms", ctypes.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class GhcmInstance(ctypes.Structure):
+    _fields_ = [
+        ("field", ctypes.c_void_p),
+        ("time_out", ctypes.c_void_p),
+        ("seeds_xy", ctypes.c_void_p),
+        ("n_seeds", ctypes.c_uint32),
+        ("width", ctypes.c_uint32),
+        ("height", ctypes.c_uint32),
+        ("h", ctypes.c_float),
+        ("input_is_speed", ctypes.c_int32),
+        ("reserved", ctypes.c_uint32),
+    ]
+
+
+class GhcmBatchInfo(ctypes.Structure):
+    _fields_ = [
+        ("instances", ctypes.c_uint32),
+        ("tiles", ctypes.c_uint32),
+        ("cells", ctypes.c_uint64),
+        ("block_size", ctypes.c_uint32),
+        ("max_jobs", ctypes.c_uint32),
+        ("max_sweeps", ctypes.c_uint32),
+        ("graph", ctypes.c_uint32),
+        ("grid", ctypes.c_uint32),
+        ("tma_instances", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 2),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
+
+
+class GhcmTuneTrial(ctypes.Structure):
+    _fields_ = [
+        ("block_size", ctypes.c_uint32),
+        ("max_jobs", ctypes.c_uint32),
+        ("max_sweeps", ctypes.c_uint32),
+        ("status", ctypes.c_int32),
+        ("ms", ctypes.c_double),
+        ("block_solves", ctypes.c_uint64),
     ]
 
     def as_dict(self) -> dict:
@@ -112,6 +164,14 @@ def load(path: Path | None = None):
     lib.ghcm_selftest_wait_timeout.argtypes = [vp, ctypes.c_uint32]
     lib.ghcm_solve_device_noalloc.argtypes = [cfgp, vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
                                               vp, ctypes.c_uint32, vp, vp]
+    instp = ctypes.POINTER(GhcmInstance)
+    lib.ghcm_batch_create.argtypes = [vp, instp, ctypes.c_uint32, ctypes.POINTER(vp)]
+    lib.ghcm_batch_run.argtypes = [vp, vp, stp]
+    lib.ghcm_batch_query.argtypes = [vp, ctypes.POINTER(GhcmBatchInfo)]
+    lib.ghcm_batch_destroy.argtypes = [vp]
+    lib.ghcm_solve_batched.argtypes = [vp, instp, ctypes.c_uint32, vp, stp]
+    lib.ghcm_autotune_batch.argtypes = [cfgp, instp, ctypes.c_uint32, vp, ctypes.c_uint32, cfgp,
+                                        ctypes.POINTER(GhcmTuneTrial), ctypes.c_uint32, u32p]
     for name in EXPORTS:
         if name != "ghcm_status_string":
             getattr(lib, name).restype = ctypes.c_int

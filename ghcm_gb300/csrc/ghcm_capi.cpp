@@ -7,8 +7,7 @@
 // The reference's per-wave host loop (priority queue, job upload, blocking
 // status read, neighbour activation) has no host counterpart here: it runs on
 // the device inside one persistent kernel (ghcm_solver.cu).
-#include "../../include/ghcm.h"
-#include "ghcm_internal.h"
+#include "ghcm_host.h"
 
 #include <algorithm>
 #include <chrono>
@@ -17,40 +16,7 @@
 #include <cstring>
 #include <new>
 
-namespace {
-
 using namespace ghcm;
-
-
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    bool reserve(size_t need) {
-        if (need <= bytes) return true;
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-        if (cudaMalloc(&p, need) != cudaSuccess) {
-            p = nullptr;
-            cudaGetLastError();
-            return false;
-        }
-        bytes = need;
-        return true;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    template <typename T>
-    T* as() const { return static_cast<T*>(p); }
-};
-
-size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
-
-}  // namespace
 
 namespace ghcm {
 
@@ -96,29 +62,7 @@ bool encode_tile_map(EncodeTiledFn encode, CUtensorMap* map, const float* base, 
 
 }  // namespace ghcm
 
-struct ghcm_ctx {
-    ghcm_config cfg;
-    int device = 0;
-    int sms = 0;
-    LaunchInfo launch{};
-    EncodeTiledFn encode = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
-    // scheduler workspace: flags | key | tmin | list0 | list1 | jobs | ctl | insts
-    DevBuf ws;
-    // field buffers used by ghcm_solve (host-pointer entry)
-    DevBuf d_in, d_time, d_seeds;
-    // pinned staging for the instance record and the control block readback
-    Inst* h_inst = nullptr;
-    Ctl* h_ctl = nullptr;
-};
-
 namespace {
-
-int map_cuda(cudaError_t e) {
-    if (e == cudaSuccess) return GHCM_OK;
-    if (e == cudaErrorMemoryAllocation) return GHCM_ERR_OOM;
-    return GHCM_ERR_CUDA;
-}
 
 struct Layout {
     size_t flags, key, tmin, list0, list1, jobs, ctl, insts, total;
@@ -142,11 +86,6 @@ Layout layout_for(uint32_t tiles, uint32_t jobs) {
     l.insts = take(sizeof(Inst));
     l.total = o;
     return l;
-}
-
-uint32_t bytes_per_solve(uint32_t b) {
-    // speed read (B^2) + time tile with its edge halo (no corners) read + time write, FP32
-    return 4u * b * b + 4u * ((b + 2u) * (b + 2u) - 4u) + 4u * b * b;
 }
 
 int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t w, uint32_t h, float spacing,
@@ -175,6 +114,8 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     I.tile_base = 0;
     I.spacing = spacing;
     I.in_is_speed = input_is_speed ? 1u : 0u;
+    I.seeds = d_seeds;
+    I.n_seeds = n_seeds;
     bool const aligned = (w % 4u == 0u) && (reinterpret_cast<uintptr_t>(d_field) % 16u == 0u) &&
                          (reinterpret_cast<uintptr_t>(d_time) % 16u == 0u);
     I.tma = 0;
@@ -193,19 +134,14 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     s.ctl = reinterpret_cast<Ctl*>(base + L.ctl);
     s.num_tiles = tiles;
     s.num_insts = 1;
-    s.max_jobs = max_jobs;
-    s.key_mode = ctx->cfg.key_mode;
-    s.max_sweeps = ctx->cfg.max_sweeps ? ctx->cfg.max_sweeps : 4u * B * B;
-    s.max_waves = ctx->cfg.max_waves;
-    s.eps = ctx->cfg.eps;
-    s.timeout_ns = static_cast<uint64_t>(ctx->cfg.wait_timeout_ms ? ctx->cfg.wait_timeout_ms : 2000u) * 1000000ull;
+    fill_sched_params(s, ctx->cfg, ctx->sms, tiles);
 
     cudaError_t e;
     if ((e = cudaMemcpyAsync(base + L.insts, &I, sizeof(Inst), cudaMemcpyHostToDevice, st)) != cudaSuccess)
         return map_cuda(e);
     if ((e = cudaMemsetAsync(s.ctl, 0, sizeof(Ctl), st)) != cudaSuccess) return map_cuda(e);
     cudaEventRecord(ctx->ev0, st);
-    if ((e = launch_init(s, &I, 1, d_seeds, nullptr, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
+    if ((e = launch_init(s, 1, static_cast<uint64_t>(w) * h, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
         return map_cuda(e);
     int const grid = ctx->launch.blocks_per_sm * ctx->sms;
     cudaEventRecord(ctx->ev2, st);
@@ -240,12 +176,7 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
         stats->tiles = tiles;
         stats->device_ms = ms;
     }
-    if (c.error & kErrBadSeed) return GHCM_ERR_BAD_ARG;
-    if (c.error & kErrBadInput) return GHCM_ERR_BAD_INPUT;
-    if (c.error & kErrTimeout) return GHCM_ERR_TIMEOUT;
-    if (c.error & kErrInternal) return GHCM_ERR_INTERNAL;
-    if (c.error & kErrNotConverged) return GHCM_ERR_NOT_CONVERGED;
-    return GHCM_OK;
+    return status_from_error(c.error);
 }
 
 int check_field_args(ghcm_ctx* ctx, const void* field, uint32_t w, uint32_t h, float spacing, const void* seeds,

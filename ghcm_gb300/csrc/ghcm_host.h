@@ -1,0 +1,91 @@
+// Host-side pieces shared by the C-ABI files (ghcm_capi.cpp, ghcm_batch.cpp):
+// the context, device buffers and status mapping. Not part of the public
+// interface.
+#pragma once
+
+#include "../../include/ghcm.h"
+#include "ghcm_internal.h"
+
+#include <cstddef>
+#include <cstdint>
+
+namespace ghcm {
+
+// A growable device allocation.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    bool reserve(size_t need) {
+        if (need <= bytes) return true;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (cudaMalloc(&p, need) != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            return false;
+        }
+        bytes = need;
+        return true;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+inline int map_cuda(cudaError_t e) {
+    if (e == cudaSuccess) return GHCM_OK;
+    if (e == cudaErrorMemoryAllocation) return GHCM_ERR_OOM;
+    return GHCM_ERR_CUDA;
+}
+
+// Ctl::error bits -> status, most specific first.
+inline int status_from_error(uint32_t error) {
+    if (error & kErrBadSeed) return GHCM_ERR_BAD_ARG;
+    if (error & kErrBadInput) return GHCM_ERR_BAD_INPUT;
+    if (error & kErrTimeout) return GHCM_ERR_TIMEOUT;
+    if (error & kErrInternal) return GHCM_ERR_INTERNAL;
+    if (error & kErrNotConverged) return GHCM_ERR_NOT_CONVERGED;
+    return GHCM_OK;
+}
+
+// Algorithmic HBM bytes of one block-solve of a B x B tile, FP32: speed read
+// (B^2) + time tile with its edge halo, no corners, read ((B+2)^2 - 4) + time
+// write (B^2).
+inline uint32_t bytes_per_solve(uint32_t b) { return 4u * b * b + 4u * ((b + 2u) * (b + 2u) - 4u) + 4u * b * b; }
+
+// Scheduler parameters of a config on a device with `sms` SMs.
+inline void fill_sched_params(Sched& s, const ghcm_config& cfg, int sms, uint32_t tiles) {
+    uint32_t const B = cfg.block_size;
+    s.max_jobs = cfg.max_jobs ? cfg.max_jobs : 8u * static_cast<uint32_t>(sms);
+    if (s.max_jobs > tiles) s.max_jobs = tiles;
+    s.key_mode = cfg.key_mode;
+    s.max_sweeps = cfg.max_sweeps ? cfg.max_sweeps : 4u * B * B;
+    s.max_waves = cfg.max_waves;
+    s.eps = cfg.eps;
+    s.timeout_ns = static_cast<uint64_t>(cfg.wait_timeout_ms ? cfg.wait_timeout_ms : 2000u) * 1000000ull;
+}
+
+}  // namespace ghcm
+
+struct ghcm_ctx {
+    ghcm_config cfg;
+    int device = 0;
+    int sms = 0;
+    ghcm::LaunchInfo launch{};
+    ghcm::EncodeTiledFn encode = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    // scheduler workspace: flags | key | tmin | list0 | list1 | jobs | ctl | insts
+    ghcm::DevBuf ws;
+    // field buffers used by ghcm_solve (host-pointer entry)
+    ghcm::DevBuf d_in, d_time, d_seeds;
+    // pinned staging for the instance record and the control block readback
+    ghcm::Inst* h_inst = nullptr;
+    ghcm::Ctl* h_ctl = nullptr;
+};

@@ -37,8 +37,10 @@ struct Inst {
     uint32_t     tile_base;  // first global tile id of this instance
     float        spacing;    // h: cost = h / speed
     uint32_t     in_is_speed;
-    int32_t      tma;        // 1: tiles of this instance are staged by TMA with the maps in Sched
-    uint32_t     cell_base_lo, cell_base_hi;  // unused by the single-grid path
+    int32_t      tma;        // 1: tiles of this instance are staged by TMA (maps in Sched)
+    const uint32_t* seeds;   // n_seeds (x, y) pairs on the device
+    uint32_t     n_seeds;
+    uint32_t     pad0;
 };
 
 // Device-side control block of one solve.
@@ -59,8 +61,9 @@ struct Ctl {
 // Everything the persistent kernel needs; passed by value as a
 // __grid_constant__ parameter so that the tensor maps sit in parameter space.
 struct Sched {
-    CUtensorMap tmap_time;         // box (B+8) x (B+2) over the time field of instance 0
+    CUtensorMap tmap_time;         // box (B+8) x (B+4) over the time field of instance 0
     CUtensorMap tmap_in;           // same box over the speed/cost field of instance 0
+    const CUtensorMap* maps;       // batches: {time, in} maps of instance i at [2i], [2i+1]; nullptr: the two above
     const Inst* insts;
     const uint32_t* tile_inst;     // per-tile instance index (nullptr: a single instance)
     uint32_t* flags;               // per-tile kActive | kFull | edge bits
@@ -100,8 +103,10 @@ bool encode_tile_map(EncodeTiledFn encode, CUtensorMap* map, const float* base, 
 int query_persistent(int block, int fim, LaunchInfo* info);
 // The staged box (elements) of a tile: the TMA tensor maps use it as their box.
 void tile_box(int block, uint32_t* width, uint32_t* height);
-cudaError_t launch_init(const Sched& s, const Inst* h_insts, uint32_t n_insts, const uint32_t* d_seeds,
-                        const uint32_t* d_seed_inst, uint32_t n_seeds, int block, cudaStream_t st);
+// Initialises the per-tile state, the time fields (+inf, inputs checked) and
+// the seeds of every instance. max_cells / max_seeds: the largest instance.
+cudaError_t launch_init(const Sched& s, uint32_t n_insts, uint64_t max_cells, uint32_t max_seeds, int block,
+                        cudaStream_t st);
 cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cudaStream_t st);
 cudaError_t launch_wait_selftest(uint32_t* flag, Ctl* ctl, uint64_t timeout_ns, cudaStream_t st);
 

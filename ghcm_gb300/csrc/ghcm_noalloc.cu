@@ -22,7 +22,7 @@
 // cudaGetSymbolAddress (with that device current); make that first call
 // before capturing any stream into a graph.
 #include "ghcm_device.cuh"
-#include "ghcm_internal.h"
+#include "ghcm_host.h"
 
 #include <algorithm>
 #include <atomic>
@@ -105,6 +105,8 @@ extern "C" int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_
     inst.tiles_y = (height + B - 1) / B;
     inst.spacing = h;
     inst.in_is_speed = input_is_speed ? 1u : 0u;
+    inst.seeds = d_seeds_xy;
+    inst.n_seeds = n_seeds;
     bool const aligned = (width % 4u == 0u) && (reinterpret_cast<uintptr_t>(d_field) % 16u == 0u) &&
                          (reinterpret_cast<uintptr_t>(d_time_out) % 16u == 0u);
     EncodeTiledFn const enc = tensor_map_encoder();
@@ -125,19 +127,14 @@ extern "C" int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_
     s.tile_inst = nullptr;
     s.num_tiles = tiles;
     s.num_insts = 1;
-    s.max_jobs = std::min<uint32_t>(cfg->max_jobs ? cfg->max_jobs : 8u * static_cast<uint32_t>(sms), tiles);
-    s.key_mode = cfg->key_mode;
-    s.max_sweeps = cfg->max_sweeps ? cfg->max_sweeps : 4u * B * B;
-    s.max_waves = cfg->max_waves;
-    s.eps = cfg->eps;
-    s.timeout_ns = static_cast<uint64_t>(cfg->wait_timeout_ms ? cfg->wait_timeout_ms : 2000u) * 1000000ull;
+    fill_sched_params(s, *cfg, sms, tiles);
 
     cudaStream_t const st = static_cast<cudaStream_t>(stream);
     cudaError_t e;
     k_store_inst<<<1, 1, 0, st>>>(d_inst, inst);
     if ((e = cudaGetLastError()) != cudaSuccess) return GHCM_ERR_CUDA;
     if ((e = cudaMemsetAsync(s.ctl, 0, sizeof(Ctl), st)) != cudaSuccess) return GHCM_ERR_CUDA;
-    if ((e = launch_init(s, &inst, 1, d_seeds_xy, nullptr, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
+    if ((e = launch_init(s, 1, static_cast<uint64_t>(width) * height, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
         return GHCM_ERR_CUDA;
     if ((e = launch_persistent(static_cast<int>(B), cfg->kernel == GHCM_KERNEL_FIM, s, li.blocks_per_sm * sms, st)) !=
         cudaSuccess)
@@ -146,10 +143,5 @@ extern "C" int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_
     if ((e = cudaMemcpyAsync(&error, &s.ctl->error, sizeof(error), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return GHCM_ERR_CUDA;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return GHCM_ERR_CUDA;
-    if (error & kErrBadSeed) return GHCM_ERR_BAD_ARG;
-    if (error & kErrBadInput) return GHCM_ERR_BAD_INPUT;
-    if (error & kErrTimeout) return GHCM_ERR_TIMEOUT;
-    if (error & kErrInternal) return GHCM_ERR_INTERNAL;
-    if (error & kErrNotConverged) return GHCM_ERR_NOT_CONVERGED;
-    return GHCM_OK;
+    return status_from_error(error);
 }

@@ -21,6 +21,15 @@ __device__ __forceinline__ uint32_t inst_of(const Sched& s, uint32_t tile) {
     return s.tile_inst ? __ldg(&s.tile_inst[tile]) : 0u;
 }
 
+// TMA tensor maps of instance ii: a batch keeps them in a device table, a
+// single solve in the kernel parameters.
+__device__ __forceinline__ const CUtensorMap* time_map(const Sched& s, uint32_t ii) {
+    return s.maps ? &s.maps[2u * ii] : &s.tmap_time;
+}
+__device__ __forceinline__ const CUtensorMap* in_map(const Sched& s, uint32_t ii) {
+    return s.maps ? &s.maps[2u * ii + 1u] : &s.tmap_in;
+}
+
 // Block id -> origin and clipped size (data/eikonal_ghcm_systolic.cl:65-97).
 template <int B>
 __device__ __forceinline__ TileCoord tile_coord(const Inst& I, uint32_t tile) {

@@ -167,54 +167,47 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
 }
 
 // ---------------------------------------------------------------------------
-// Initialisation kernels (src/eikonal_hcm.cpp:189-238).
+// Initialisation kernels (src/eikonal_hcm.cpp:189-238). blockIdx.y is the
+// instance; a single solve is a batch of one.
 // ---------------------------------------------------------------------------
-__global__ void k_init_tiles(Sched s) {
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < s.num_tiles; t += gridDim.x * blockDim.x) {
-        s.flags[t] = 0u;
-        s.key[t] = inf_bits();
-        s.tmin[t] = f_inf();
-    }
-}
 
-// time = +inf everywhere; rejects NaN or negative inputs.
-__global__ void k_init_field(const Inst* insts, uint32_t inst, Ctl* ctl) {
-    Inst const I = insts[inst];
+// Per-tile scheduler state and instance index, time = +inf everywhere; rejects
+// NaN or negative inputs.
+__global__ void k_init_inst(Sched s) {
+    Inst const I = s.insts[blockIdx.y];
+    uint32_t const stride = gridDim.x * blockDim.x;
+    uint32_t const first = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t const n_tiles = I.tiles_x * I.tiles_y;
+    for (uint32_t t = first; t < n_tiles; t += stride) {
+        uint32_t const g = I.tile_base + t;
+        s.flags[g] = 0u;
+        s.key[g] = inf_bits();
+        s.tmin[g] = f_inf();
+        if (s.tile_inst) const_cast<uint32_t*>(s.tile_inst)[g] = blockIdx.y;
+    }
     size_t const n = static_cast<size_t>(I.w) * I.h;
     bool bad = false;
-    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    for (size_t i = first; i < n; i += stride) {
         float const v = __ldg(&I.in[i]);
         bad |= !(v >= 0.f);
         I.time[i] = f_inf();
     }
-    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctl->error, kErrBadInput);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&s.ctl->error, kErrBadInput);
 }
 
 // Seeds: time 0, and the tiles of their 4-neighbours become active with key 0
 // (seed_map and the initial heap, src/eikonal_hcm.cpp:198-238).
-__global__ void k_init_seeds(Sched s, const uint32_t* seeds, const uint32_t* seed_inst, uint32_t n_seeds,
-                             int block) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_seeds; i += gridDim.x * blockDim.x) {
-        uint32_t const ii = seed_inst ? seed_inst[i] : 0u;
-        const Inst& I = s.insts[ii];
-        uint32_t const x = seeds[2 * i], y = seeds[2 * i + 1];
-        if (x >= I.w || y >= I.h) {
+__global__ void k_init_seeds(Sched s, int block) {
+    constexpr int dir[4][2] = {{-1, 0}, {0, -1}, {1, 0}, {0, 1}};
+    Inst const I = s.insts[blockIdx.y];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < I.n_seeds; i += gridDim.x * blockDim.x) {
+        uint32_t const ux = I.seeds[2 * i], uy = I.seeds[2 * i + 1];
+        if (ux >= I.w || uy >= I.h) {
             atomicOr(&s.ctl->error, kErrBadSeed);
             continue;
         }
-        I.time[static_cast<size_t>(y) * I.w + x] = 0.f;
-    }
-}
-
-__global__ void k_activate_seeds(Sched s, const uint32_t* seeds, const uint32_t* seed_inst, uint32_t n_seeds,
-                                 int block) {
-    constexpr int dir[4][2] = {{-1, 0}, {0, -1}, {1, 0}, {0, 1}};
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_seeds; i += gridDim.x * blockDim.x) {
-        uint32_t const ii = seed_inst ? seed_inst[i] : 0u;
-        const Inst& I = s.insts[ii];
-        int const x = static_cast<int>(seeds[2 * i]), y = static_cast<int>(seeds[2 * i + 1]);
-        if (x >= static_cast<int>(I.w) || y >= static_cast<int>(I.h)) continue;
+        I.time[static_cast<size_t>(uy) * I.w + ux] = 0.f;
+        int const x = static_cast<int>(ux), y = static_cast<int>(uy);
         for (auto const& d : dir) {
             int const px = x + d[0], py = y + d[1];
             if (px < 0 || py < 0 || px >= static_cast<int>(I.w) || py >= static_cast<int>(I.h)) continue;
@@ -299,21 +292,19 @@ int query_persistent(int block, int fim, LaunchInfo* info) {
     return 0;
 }
 
-cudaError_t launch_init(const Sched& s, const Inst* h_insts, uint32_t n_insts, const uint32_t* d_seeds,
-                        const uint32_t* d_seed_inst, uint32_t n_seeds, int block, cudaStream_t st) {
+cudaError_t launch_init(const Sched& s, uint32_t n_insts, uint64_t max_cells, uint32_t max_seeds, int block,
+                        cudaStream_t st) {
+    if (n_insts == 0u || n_insts > 65535u) return cudaErrorInvalidValue;
     unsigned const tb = 256;
-    unsigned const tiles_grid = static_cast<unsigned>(std::min<uint32_t>((s.num_tiles + tb - 1) / tb, 4096u));
-    k_init_tiles<<<std::max(1u, tiles_grid), tb, 0, st>>>(s);
-    for (uint32_t i = 0; i < n_insts; ++i) {
-        size_t const cells = static_cast<size_t>(h_insts[i].w) * h_insts[i].h;
-        unsigned const g = static_cast<unsigned>(std::min<size_t>((cells + tb - 1) / tb, 152u * 16u));
-        k_init_field<<<std::max(1u, g), tb, 0, st>>>(s.insts, i, s.ctl);
-    }
-    if (n_seeds) {
+    // about 16 CTAs per SM over the whole batch, at least 8 per instance
+    uint64_t const want = (max_cells + tb - 1) / tb;
+    unsigned const per = static_cast<unsigned>(std::max<uint64_t>(8u, 152u * 16u * 4u / n_insts));
+    unsigned const gx = static_cast<unsigned>(std::max<uint64_t>(1u, std::min<uint64_t>(want, per)));
+    k_init_inst<<<dim3(gx, n_insts), tb, 0, st>>>(s);
+    if (max_seeds) {
         unsigned const sb = 128;
-        unsigned const g = static_cast<unsigned>(std::min<uint32_t>((n_seeds + sb - 1) / sb, 1024u));
-        k_init_seeds<<<g, sb, 0, st>>>(s, d_seeds, d_seed_inst, n_seeds, block);
-        k_activate_seeds<<<g, sb, 0, st>>>(s, d_seeds, d_seed_inst, n_seeds, block);
+        unsigned const gs = std::min<unsigned>((max_seeds + sb - 1) / sb, 64u);
+        k_init_seeds<<<dim3(gs, n_insts), sb, 0, st>>>(s, block);
     }
     return cudaGetLastError();
 }
@@ -322,7 +313,19 @@ cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cuda
     void* k = select_kernel(block, fim);
     if (!k) return cudaErrorInvalidValue;
     void* args[] = {const_cast<Sched*>(&s)};
-    return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(threads_for(block, fim)), args, 0, st);
+    // A cooperative launch guarantees the co-residency the grid barrier needs;
+    // through cudaLaunchKernelExC it can also be captured into a CUDA graph.
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(threads_for(block, fim));
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, k, args);
 }
 
 cudaError_t launch_wait_selftest(uint32_t* flag, Ctl* ctl, uint64_t timeout_ns, cudaStream_t st) {

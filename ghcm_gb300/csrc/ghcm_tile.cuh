@@ -67,7 +67,8 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
                            uint32_t& parity, bool& tma_pending, uint32_t* s_word, float* s_red) {
     using G = TileGeom<B>;
     int const tid = threadIdx.x;
-    const Inst& I = s.insts[inst_of(s, tile)];
+    uint32_t const ii = inst_of(s, tile);
+    const Inst& I = s.insts[ii];
     TileCoord const tc = tile_coord<B>(I, tile);
     bool const use_tma = I.tma != 0;
 
@@ -83,8 +84,8 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
         if (use_tma) {
             fence_proxy_async();
             mbar_arrive_expect_tx(bar, static_cast<uint32_t>(2 * G::BOX * sizeof(float)));
-            tma_load_2d(sm.time, &s.tmap_time, bar, tc.ox - 4, tc.oy - 2);
-            tma_load_2d(sm.cost, &s.tmap_in, bar, tc.ox - 4, tc.oy - 2);
+            tma_load_2d(sm.time, time_map(s, ii), bar, tc.ox - 4, tc.oy - 2);
+            tma_load_2d(sm.cost, in_map(s, ii), bar, tc.ox - 4, tc.oy - 2);
             tma_pending = true;
         }
     }

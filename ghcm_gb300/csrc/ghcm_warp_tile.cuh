@@ -47,7 +47,8 @@ __device__ bool solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, War
     int const lane = threadIdx.x & 31;
     int const x = lane % B;
     int const band = lane / B;
-    const Inst& I = s.insts[inst_of(s, tile)];
+    uint32_t const ii = inst_of(s, tile);
+    const Inst& I = s.insts[ii];
     TileCoord const tc = tile_coord<B>(I, tile);
     bool const use_tma = I.tma != 0;
 
@@ -59,8 +60,8 @@ __device__ bool solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, War
         if (use_tma) {
             fence_proxy_async();
             mbar_arrive_expect_tx(&sm.bar, static_cast<uint32_t>(2 * G::BOX * sizeof(float)));
-            tma_load_2d(sm.time, &s.tmap_time, &sm.bar, tc.ox - 4, tc.oy - 2);
-            tma_load_2d(sm.cost, &s.tmap_in, &sm.bar, tc.ox - 4, tc.oy - 2);
+            tma_load_2d(sm.time, time_map(s, ii), &sm.bar, tc.ox - 4, tc.oy - 2);
+            tma_load_2d(sm.cost, in_map(s, ii), &sm.bar, tc.ox - 4, tc.oy - 2);
             tma_pending = true;
         }
     }

@@ -114,6 +114,84 @@ int ghcm_solve_device(ghcm_ctx* ctx, const float* d_field, int input_is_speed, u
                       uint32_t height, float h, const uint32_t* d_seeds_xy, uint32_t n_seeds,
                       float* d_time_out, void* stream, ghcm_stats* stats);
 
+/* ---- batches: many independent instances in one persistent launch ----
+ * No counterpart in the reference, which solves one field per call
+ * (src/eikonal_hcm.cpp:186-529). Every instance is one reference solve
+ * (eikonal_hcm_opencl_ex) with its own field, seeds and spacing; the tiles of
+ * all instances share one device scheduler (one active set ordered by key,
+ * n = cfg.max_jobs jobs per wave over the whole batch) and one persistent grid,
+ * so small instances no longer leave the GPU idle. The launch sequence is
+ * captured once in a CUDA graph and replayed by ghcm_batch_run. */
+
+typedef struct ghcm_instance {
+    const float*    field;          /* device: width*height speed (input_is_speed = 1) or cost */
+    float*          time_out;       /* device: width*height arrival times (written) */
+    const uint32_t* seeds_xy;       /* device: n_seeds (x, y) pairs */
+    uint32_t        n_seeds;
+    uint32_t        width, height;
+    float           h;              /* grid spacing: cost = h / speed */
+    int32_t         input_is_speed;
+    uint32_t        reserved;       /* must be zero */
+} ghcm_instance;
+
+typedef struct ghcm_batch_info {
+    uint32_t instances;
+    uint32_t tiles;                 /* tiles over all instances */
+    uint64_t cells;                 /* cells over all instances */
+    uint32_t block_size;
+    uint32_t max_jobs;              /* n per wave over the whole batch */
+    uint32_t max_sweeps;
+    uint32_t graph;                 /* 1: ghcm_batch_run replays a CUDA graph; 0: it launches directly */
+    uint32_t grid;                  /* CTAs of the persistent launch */
+    uint32_t tma_instances;         /* instances staged by TMA (the rest use plain loads) */
+    uint32_t reserved[2];
+} ghcm_batch_info;
+
+typedef struct ghcm_batch ghcm_batch;
+
+/* Validates the instances, allocates the batch's scheduler workspace and
+ * captures its launch sequence (init + persistent solve + status readback)
+ * into a CUDA graph. The instance buffers are the caller's and must stay
+ * valid until ghcm_batch_destroy. Up to 65535 instances. Uses ctx's config
+ * and device; the batch is independent of later calls on ctx. */
+int ghcm_batch_create(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count, ghcm_batch** out);
+
+/* Solves every instance of the batch on `stream` (a cudaStream_t) and returns
+ * when it has finished. stats (optional) cover the whole batch:
+ * cells = sum of instance cells, device_ms = time of the replay. */
+int ghcm_batch_run(ghcm_batch* batch, void* stream, ghcm_stats* stats);
+
+int ghcm_batch_query(const ghcm_batch* batch, ghcm_batch_info* out);
+
+/* Releases a batch. NULL is accepted. */
+int ghcm_batch_destroy(ghcm_batch* batch);
+
+/* create + run + destroy. */
+int ghcm_solve_batched(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count, void* stream, ghcm_stats* stats);
+
+/* One autotuner trial. */
+typedef struct ghcm_tune_trial {
+    uint32_t block_size;
+    uint32_t max_jobs;
+    uint32_t max_sweeps;            /* 0 = to convergence (4 * block_size^2 cap) */
+    int32_t  status;                /* GHCM_OK or the failing status */
+    double   ms;                    /* best device time of the replays */
+    uint64_t block_solves;
+} ghcm_tune_trial;
+
+/* Picks tile size (8, 16, 32), n and the inner-sweep cap for a batch by
+ * timing CUDA-graph replays of it, starting from `base`: tile size x n on the
+ * grid {8, 16, 32} x {4, 16, 64} x SMs, then n halved and doubled around the
+ * best, then the inner-sweep caps B/2, B, 2B (14 trials).
+ * Writes the fastest config to *best and the trials run to
+ * trials[0..max_trials) (*n_trials = how many ran; trials may be NULL). The
+ * instances' time_out fields hold a converged solve on return. reps >= 1
+ * timed replays per trial after one warm-up. No counterpart in the reference
+ * (its harness sweeps block sizes by hand, src/test_runner.cpp:226-291). */
+int ghcm_autotune_batch(const ghcm_config* base, const ghcm_instance* insts, uint32_t count, void* stream,
+                        uint32_t reps, ghcm_config* best, ghcm_tune_trial* trials, uint32_t max_trials,
+                        uint32_t* n_trials);
+
 /* Number of SMs of the context's device (the reference's compute units). */
 int ghcm_device_sm_count(const ghcm_ctx* ctx, uint32_t* out);
 

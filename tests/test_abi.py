@@ -38,14 +38,19 @@ def test_struct_layouts_match_c(tmp_path):
     src = tmp_path / "sizes.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "ghcm.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu\\n\", sizeof(ghcm_config), sizeof(ghcm_stats),"
-        " offsetof(ghcm_stats, device_ms), offsetof(ghcm_config, use_tma)); return 0;}\n")
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(ghcm_config), sizeof(ghcm_stats),"
+        " offsetof(ghcm_stats, device_ms), offsetof(ghcm_config, use_tma), sizeof(ghcm_instance),"
+        " offsetof(ghcm_instance, input_is_speed), sizeof(ghcm_batch_info), offsetof(ghcm_batch_info, tma_instances),"
+        " sizeof(ghcm_tune_trial), offsetof(ghcm_tune_trial, ms)); return 0;}\n")
     exe = tmp_path / "sizes"
     subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
                    check=True)
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert got == [ctypes.sizeof(_lib.GhcmConfig), ctypes.sizeof(_lib.GhcmStats),
-                   _lib.GhcmStats.device_ms.offset, _lib.GhcmConfig.use_tma.offset]
+                   _lib.GhcmStats.device_ms.offset, _lib.GhcmConfig.use_tma.offset,
+                   ctypes.sizeof(_lib.GhcmInstance), _lib.GhcmInstance.input_is_speed.offset,
+                   ctypes.sizeof(_lib.GhcmBatchInfo), _lib.GhcmBatchInfo.tma_instances.offset,
+                   ctypes.sizeof(_lib.GhcmTuneTrial), _lib.GhcmTuneTrial.ms.offset]
 
 
 def test_header_compiles_as_cpp(tmp_path):
@@ -114,3 +119,25 @@ def test_python_interface_reports_missing_gpu():
     assert g.eikonal_hcm_cuda_setup(g.HcmConfig()) is None
     with pytest.raises(g.GhcmError):
         g.HcmSetup(g.HcmConfig())
+
+
+def test_batch_calls_check_arguments(ghcm_lib):
+    b = ctypes.c_void_p()
+    inst = (_lib.GhcmInstance * 1)()
+    assert ghcm_lib.ghcm_batch_create(None, inst, 1, ctypes.byref(b)) == _lib.GHCM_ERR_BAD_ARG
+    assert ghcm_lib.ghcm_batch_create(None, inst, 1, None) == _lib.GHCM_ERR_BAD_ARG
+    assert ghcm_lib.ghcm_batch_run(None, None, None) == _lib.GHCM_ERR_BAD_ARG
+    info = _lib.GhcmBatchInfo()
+    assert ghcm_lib.ghcm_batch_query(None, ctypes.byref(info)) == _lib.GHCM_ERR_BAD_ARG
+    assert ghcm_lib.ghcm_batch_destroy(None) == 0
+    assert ghcm_lib.ghcm_solve_batched(None, inst, 1, None, None) == _lib.GHCM_ERR_BAD_ARG
+    c = _lib.GhcmConfig()
+    ghcm_lib.ghcm_config_default(ctypes.byref(c))
+    best = _lib.GhcmConfig()
+    n = ctypes.c_uint32()
+    assert ghcm_lib.ghcm_autotune_batch(ctypes.byref(c), None, 0, None, 1, ctypes.byref(best), None, 0,
+                                        ctypes.byref(n)) == _lib.GHCM_ERR_BAD_ARG
+    bad = _lib.GhcmConfig.from_buffer_copy(c)
+    bad.block_size = 24
+    assert ghcm_lib.ghcm_autotune_batch(ctypes.byref(bad), inst, 1, None, 1, ctypes.byref(best), None, 0,
+                                        ctypes.byref(n)) == _lib.GHCM_ERR_BAD_ARG
