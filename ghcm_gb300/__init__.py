@@ -26,3 +26,4 @@ from .batch import (  # noqa: F401
     solve_batched,
     solve_sharded,
 )
+from . import learned  # noqa: F401

@@ -43,7 +43,22 @@ EXPORTS = (
     "ghcm_batch_destroy",
     "ghcm_solve_batched",
     "ghcm_autotune_batch",
+    "ghcm_trace_enable",
+    "ghcm_trace_read",
+    "ghcm_set_schedule_model",
+    "ghcm_set_schedule_policy",
+    "ghcm_schedule_counters",
+    "ghcm_mlp_forward",
+    "ghcm_mlp_grad",
+    "ghcm_train_config_default",
+    "ghcm_mlp_train",
 )
+
+GHCM_MLP_FEATURES = 12
+GHCM_MLP_HIDDEN = 64
+GHCM_MLP_PARAMS = 5057
+GHCM_POLICY_SCORE = 0
+GHCM_POLICY_VETO = 1
 
 
 class GhcmConfig(ctypes.Structure):
@@ -59,7 +74,8 @@ class GhcmConfig(ctypes.Structure):
         ("wait_timeout_ms", ctypes.c_uint32),
         ("device", ctypes.c_int32),
         ("use_tma", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32 * 5),
+        ("fallback_jobs", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 4),
     ]
 
 
@@ -127,6 +143,29 @@ class GhcmTuneTrial(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class GhcmTraceRecord(ctypes.Structure):
+    _fields_ = [
+        ("features", ctypes.c_float * 12),
+        ("tile", ctypes.c_uint32),
+        ("wave", ctypes.c_uint32),
+        ("useful", ctypes.c_uint32),
+        ("sweeps", ctypes.c_uint32),
+    ]
+
+
+class GhcmTrainConfig(ctypes.Structure):
+    _fields_ = [
+        ("epochs", ctypes.c_uint32),
+        ("batch", ctypes.c_uint32),
+        ("lr", ctypes.c_float),
+        ("beta1", ctypes.c_float),
+        ("beta2", ctypes.c_float),
+        ("adam_eps", ctypes.c_float),
+        ("pos_weight", ctypes.c_float),
+        ("reserved", ctypes.c_uint32 * 5),
+    ]
+
+
 class GhcmError(RuntimeError):
     def __init__(self, status: int, what: str = ""):
         self.status = status
@@ -172,6 +211,16 @@ def load(path: Path | None = None):
     lib.ghcm_solve_batched.argtypes = [vp, instp, ctypes.c_uint32, vp, stp]
     lib.ghcm_autotune_batch.argtypes = [cfgp, instp, ctypes.c_uint32, vp, ctypes.c_uint32, cfgp,
                                         ctypes.POINTER(GhcmTuneTrial), ctypes.c_uint32, u32p]
+    lib.ghcm_trace_enable.argtypes = [vp, ctypes.c_uint32]
+    lib.ghcm_trace_read.argtypes = [vp, ctypes.c_void_p, ctypes.c_uint32, u32p, u32p]
+    lib.ghcm_set_schedule_model.argtypes = [vp, f32p, ctypes.c_uint32, ctypes.c_float]
+    lib.ghcm_schedule_counters.argtypes = [vp, u32p]
+    lib.ghcm_set_schedule_policy.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32]
+    lib.ghcm_mlp_forward.argtypes = [vp, vp, ctypes.c_uint32, vp, vp]
+    lib.ghcm_mlp_grad.argtypes = [vp, vp, vp, ctypes.c_uint32, ctypes.c_float, vp, vp, vp]
+    tcp = ctypes.POINTER(GhcmTrainConfig)
+    lib.ghcm_train_config_default.argtypes = [tcp]
+    lib.ghcm_mlp_train.argtypes = [vp, vp, ctypes.c_uint32, vp, tcp, vp, f32p]
     for name in EXPORTS:
         if name != "ghcm_status_string":
             getattr(lib, name).restype = ctypes.c_int

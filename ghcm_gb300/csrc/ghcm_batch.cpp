@@ -141,6 +141,8 @@ int ghcm_batch_create(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count,
         max_seeds = std::max(max_seeds, I.n_seeds);
         if (tiles >= (1ull << 31)) return GHCM_ERR_UNSUPPORTED;
     }
+    bool const learned = ctx->cfg.schedule == GHCM_SCHEDULE_LEARNED;
+    if (learned && !ctx->has_model) return GHCM_ERR_BAD_ARG;  // no schedule model set
     if (cudaSetDevice(ctx->device) != cudaSuccess) return GHCM_ERR_CUDA;
 
     ghcm_batch* b = new (std::nothrow) ghcm_batch();
@@ -187,6 +189,8 @@ int ghcm_batch_create(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count,
     size_t const o_ti = take(t4), o_jobs = take(sizeof(uint32_t) * std::max<uint32_t>(s.max_jobs, 1u));
     size_t const o_ctl = take(sizeof(Ctl)), o_insts = take(sizeof(Inst) * count);
     size_t const o_maps = take(sizeof(CUtensorMap) * 2u * count);
+    size_t const o_learn = learned ? take(learn_bytes(b->tiles)) : 0;
+    size_t const o_model = learned ? take(sizeof(float) * kParams) : 0;
     int rc = GHCM_OK;
     if (!b->ws.reserve(o)) rc = GHCM_ERR_OOM;
     if (rc == GHCM_OK && cudaMallocHost(reinterpret_cast<void**>(&b->h_ctl), sizeof(Ctl)) != cudaSuccess)
@@ -209,7 +213,16 @@ int ghcm_batch_create(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count,
     s.ctl = reinterpret_cast<Ctl*>(base + o_ctl);
     s.insts = reinterpret_cast<const Inst*>(base + o_insts);
     s.maps = b->tma_insts ? reinterpret_cast<const CUtensorMap*>(base + o_maps) : nullptr;
-    cudaError_t e = cudaMemcpy(base + o_insts, h.data(), sizeof(Inst) * count, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaSuccess;
+    if (learned) {
+        bind_learn_arrays(s.learn, base + o_learn, b->tiles);
+        s.learn.params = reinterpret_cast<const float*>(base + o_model);
+        s.learn.threshold = ctx->threshold;
+        s.learn.veto = ctx->policy == GHCM_POLICY_VETO ? 1u : 0u;
+        s.learn.max_vetoes = ctx->max_vetoes;
+        e = cudaMemcpy(base + o_model, ctx->d_model.p, sizeof(float) * kParams, cudaMemcpyDeviceToDevice);
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(base + o_insts, h.data(), sizeof(Inst) * count, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(base + o_maps, maps.data(), sizeof(CUtensorMap) * 2u * count, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {

@@ -135,6 +135,22 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     s.num_tiles = tiles;
     s.num_insts = 1;
     fill_sched_params(s, ctx->cfg, ctx->sms, tiles);
+    bool const learned = ctx->cfg.schedule == GHCM_SCHEDULE_LEARNED;
+    if (learned && !ctx->has_model) return GHCM_ERR_BAD_ARG;  // no schedule model set
+    if (learned || ctx->trace_cap) {
+        if (!ctx->d_learn.reserve(learn_bytes(tiles))) return GHCM_ERR_OOM;
+        bind_learn_arrays(s.learn, ctx->d_learn.as<char>(), tiles);
+        if (learned) {
+            s.learn.params = ctx->d_model.as<float>();
+            s.learn.threshold = ctx->threshold;
+            s.learn.veto = ctx->policy == GHCM_POLICY_VETO ? 1u : 0u;
+            s.learn.max_vetoes = ctx->max_vetoes;
+        }
+        if (ctx->trace_cap) {
+            s.learn.trace = ctx->d_trace.as<TraceRec>();
+            s.learn.trace_cap = ctx->trace_cap;
+        }
+    }
 
     cudaError_t e;
     if ((e = cudaMemcpyAsync(base + L.insts, &I, sizeof(Inst), cudaMemcpyHostToDevice, st)) != cudaSuccess)
@@ -153,6 +169,11 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return map_cuda(e);
 
     Ctl const& c = *ctx->h_ctl;
+    ctx->trace_total = c.trace_count;
+    ctx->counters[0] = c.score_waves;
+    ctx->counters[1] = c.fallback_waves;
+    ctx->counters[2] = c.trace_count;
+    ctx->counters[3] = c.vetoes;
 #ifdef GHCM_PROFILE
     std::fprintf(stderr,
                  "[ghcm-prof] grid %d solves %llu waves %u residual_passes %u kernel_us %.1f | per wave: "
@@ -275,6 +296,9 @@ int ghcm_destroy(ghcm_ctx* ctx) {
     ctx->d_in.release();
     ctx->d_time.release();
     ctx->d_seeds.release();
+    ctx->d_learn.release();
+    ctx->d_trace.release();
+    ctx->d_model.release();
     if (ctx->h_inst) cudaFreeHost(ctx->h_inst);
     if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -330,6 +354,67 @@ int ghcm_solve(ghcm_ctx* ctx, const float* field, int input_is_speed, uint32_t w
     }
     if (stats) stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return rc;
+}
+
+int ghcm_trace_enable(ghcm_ctx* ctx, uint32_t capacity) {
+    if (!ctx) return GHCM_ERR_BAD_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return GHCM_ERR_CUDA;
+    if (capacity == 0u) {
+        ctx->d_trace.release();
+        ctx->trace_cap = 0u;
+        return GHCM_OK;
+    }
+    if (!ctx->d_trace.reserve(static_cast<size_t>(capacity) * sizeof(TraceRec))) return GHCM_ERR_OOM;
+    ctx->trace_cap = capacity;
+    ctx->trace_total = 0u;
+    return GHCM_OK;
+}
+
+int ghcm_trace_read(ghcm_ctx* ctx, ghcm_trace_record* out, uint32_t max_records, uint32_t* n_records,
+                    uint32_t* n_total) {
+    if (!ctx || !n_records || (max_records && !out)) return GHCM_ERR_BAD_ARG;
+    uint32_t const have = std::min(ctx->trace_total, ctx->trace_cap);
+    uint32_t const n = std::min(have, max_records);
+    *n_records = 0u;
+    if (n_total) *n_total = ctx->trace_total;
+    if (n == 0u) return GHCM_OK;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return GHCM_ERR_CUDA;
+    cudaError_t const e = cudaMemcpy(out, ctx->d_trace.p, static_cast<size_t>(n) * sizeof(TraceRec),
+                                     cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return map_cuda(e);
+    *n_records = n;
+    return GHCM_OK;
+}
+
+int ghcm_set_schedule_model(ghcm_ctx* ctx, const float* params, uint32_t n_params, float threshold) {
+    if (!ctx) return GHCM_ERR_BAD_ARG;
+    if (!params) {
+        ctx->has_model = false;
+        return GHCM_OK;
+    }
+    if (n_params != GHCM_MLP_PARAMS || !(threshold > 0.f && threshold < 1.f)) return GHCM_ERR_BAD_ARG;
+    for (uint32_t i = 0; i < n_params; ++i)
+        if (!std::isfinite(params[i])) return GHCM_ERR_BAD_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return GHCM_ERR_CUDA;
+    if (!ctx->d_model.reserve(sizeof(float) * GHCM_MLP_PARAMS)) return GHCM_ERR_OOM;
+    cudaError_t const e = cudaMemcpy(ctx->d_model.p, params, sizeof(float) * GHCM_MLP_PARAMS, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return map_cuda(e);
+    ctx->has_model = true;
+    ctx->threshold = threshold;
+    return GHCM_OK;
+}
+
+int ghcm_set_schedule_policy(ghcm_ctx* ctx, uint32_t policy, uint32_t max_vetoes) {
+    if (!ctx || policy > GHCM_POLICY_VETO || max_vetoes > 1000u) return GHCM_ERR_BAD_ARG;
+    ctx->policy = policy;
+    ctx->max_vetoes = max_vetoes ? max_vetoes : 2u;
+    return GHCM_OK;
+}
+
+int ghcm_schedule_counters(const ghcm_ctx* ctx, uint32_t out[4]) {
+    if (!ctx || !out) return GHCM_ERR_BAD_ARG;
+    for (int i = 0; i < 4; ++i) out[i] = ctx->counters[i];
+    return GHCM_OK;
 }
 
 int ghcm_selftest_wait_timeout(ghcm_ctx* ctx, uint32_t timeout_ms) {

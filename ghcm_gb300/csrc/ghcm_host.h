@@ -39,6 +39,25 @@ struct DevBuf {
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+static_assert(kParams == GHCM_MLP_PARAMS && kFeatures == GHCM_MLP_FEATURES && kHidden == GHCM_MLP_HIDDEN,
+              "MLP shape differs from the C ABI");
+static_assert(sizeof(TraceRec) == sizeof(ghcm_trace_record), "trace record layout differs from the C ABI");
+
+// Bytes of the per-tile learning arrays (tstat | kmax | nsolve | last_change | vetoes).
+inline size_t learn_bytes(uint32_t tiles) {
+    return align_up(16ull * tiles, 256) + 4 * align_up(4ull * tiles, 256);
+}
+
+// Points s.learn's per-tile arrays into `base` (learn_bytes(tiles) bytes).
+inline void bind_learn_arrays(Learn& L, char* base, uint32_t tiles) {
+    size_t const a = align_up(16ull * tiles, 256), b = align_up(4ull * tiles, 256);
+    L.tstat = reinterpret_cast<float4*>(base);
+    L.kmax = reinterpret_cast<uint32_t*>(base + a);
+    L.nsolve = reinterpret_cast<uint32_t*>(base + a + b);
+    L.last_change = reinterpret_cast<uint32_t*>(base + a + 2 * b);
+    L.vetoes = reinterpret_cast<uint32_t*>(base + a + 3 * b);
+}
+
 inline int map_cuda(cudaError_t e) {
     if (e == cudaSuccess) return GHCM_OK;
     if (e == cudaErrorMemoryAllocation) return GHCM_ERR_OOM;
@@ -69,6 +88,7 @@ inline void fill_sched_params(Sched& s, const ghcm_config& cfg, int sms, uint32_
     s.max_sweeps = cfg.max_sweeps ? cfg.max_sweeps : 4u * B * B;
     s.max_waves = cfg.max_waves;
     s.eps = cfg.eps;
+    s.learn.fallback_jobs = cfg.fallback_jobs ? cfg.fallback_jobs : s.max_jobs;
     s.timeout_ns = static_cast<uint64_t>(cfg.wait_timeout_ms ? cfg.wait_timeout_ms : 2000u) * 1000000ull;
 }
 
@@ -88,4 +108,15 @@ struct ghcm_ctx {
     // pinned staging for the instance record and the control block readback
     ghcm::Inst* h_inst = nullptr;
     ghcm::Ctl* h_ctl = nullptr;
+    // learned schedule and trace recorder
+    ghcm::DevBuf d_learn;          // per-tile learning arrays
+    ghcm::DevBuf d_trace;          // trace records
+    uint32_t trace_cap = 0;
+    uint32_t trace_total = 0;      // records the last solve produced (may exceed trace_cap)
+    ghcm::DevBuf d_model;          // MLP parameters
+    bool has_model = false;
+    float threshold = 0.5f;
+    uint32_t policy = GHCM_POLICY_SCORE;
+    uint32_t max_vetoes = 2;
+    uint32_t counters[4] = {0, 0, 0, 0};
 };

@@ -49,6 +49,14 @@ struct Ctl {
     uint32_t bar_count;            // CTAs arrived at the current wave barrier
     uint32_t error;                // kErr* bits
     uint32_t count[2];             // sizes of the two active lists
+    uint32_t krange[2][2];         // per list: {min, max} key bits of its tiles (a superset range)
+    float    wave_front;           // smallest key of the set being scheduled this wave
+    float    wave_span;            // its key range (max - min, > 0)
+    uint32_t take_count;           // learned schedule: tiles the score phase took
+    uint32_t trace_count;          // trace records written (may exceed the capacity)
+    uint32_t score_waves;          // learned schedule: waves chosen by score
+    uint32_t fallback_waves;       // learned schedule: waves that fell back to the plain top-n
+    uint32_t vetoes;               // learned schedule, veto mode: claims deferred by the model
     uint32_t waves;
     uint32_t residual_passes;
     uint32_t max_active;
@@ -56,6 +64,44 @@ struct Ctl {
     unsigned long long prof[16];   // GHCM_PROFILE builds: per-phase nanoseconds and sweep counts
     unsigned long long release_ns; // GHCM_PROFILE builds: when the last barrier was released
     uint32_t wave_max_sweeps;      // GHCM_PROFILE builds: most sweeps of one block-solve in this wave
+};
+
+// Learned block schedule and trace recorder (see ghcm_learn.cuh).
+constexpr int kFeatures = 12;
+constexpr int kHidden = 64;
+// MLP parameters, flat: W1 [in][hidden], b1, W2 [hidden][hidden] (in-major),
+// b2, W3 [hidden], b3.
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kFeatures * kHidden;
+constexpr int kOffW2 = kOffB1 + kHidden;
+constexpr int kOffB2 = kOffW2 + kHidden * kHidden;
+constexpr int kOffW3 = kOffB2 + kHidden;
+constexpr int kOffB3 = kOffW3 + kHidden;
+constexpr int kParams = kOffB3 + 1;
+
+// One block-solve of a trace: the features the scheduler saw when it chose
+// the tile, and what the solve did. Layout = ghcm_trace_record.
+struct TraceRec {
+    float    f[kFeatures];
+    uint32_t tile;
+    uint32_t wave;
+    uint32_t useful;   // 1: the solve moved some cell by more than eps
+    uint32_t sweeps;
+};
+
+struct Learn {
+    float4*   tstat;       // per tile: feature 4-6 (log speeds), set at init; nullptr: learning off
+    uint32_t* kmax;        // per tile: largest activation key since its last claim (float bits)
+    uint32_t* nsolve;      // per tile: block-solves so far
+    uint32_t* last_change; // per tile: wave of its last useful solve + 1 (0: none)
+    uint32_t* vetoes;      // per tile: consecutive vetoes (veto mode)
+    const float* params;   // MLP parameters (kParams floats); nullptr: plain schedule
+    TraceRec* trace;       // trace records; nullptr: no trace
+    uint32_t  trace_cap;
+    float     threshold;   // take a tile when its score >= threshold
+    uint32_t  fallback_jobs;  // n of the plain top-n when no tile qualifies
+    uint32_t  veto;           // 1: the plain top-n proposes and the model vetoes at claim time
+    uint32_t  max_vetoes;     // consecutive vetoes allowed per tile before it must be solved
 };
 
 // Everything the persistent kernel needs; passed by value as a
@@ -81,6 +127,7 @@ struct Sched {
     float     eps;
     uint32_t  pad0;
     uint64_t  timeout_ns;
+    Learn     learn;
 };
 
 // Launch configuration chosen by the host for a (block size, kernel) pair.

@@ -1,0 +1,277 @@
+// Learned block schedule: per-tile features, the warp-cooperative MLP that
+// scores a tile, and the score phase that partitions an active set by score.
+//
+// The reference picks the n tiles with the smallest frozen min-time key
+// (src/eikonal_hcm.cpp:47-80, 344-358). The learned schedule scores every
+// active tile with a 12 -> 64 -> 64 -> 1 FP32 MLP estimating P(the solve moves
+// some cell by more than eps) and solves those scoring at or above a
+// threshold (tiles re-queued by the residual judge or a sweep cap always
+// go); if none qualifies it falls back to the plain top-n. The global Godunov
+// residual judge is unchanged, so a wrong score costs work, never accuracy.
+//
+// The same features are written, with the outcome of each solve, by the
+// trace recorder of the plain solver; the model is trained on those traces
+// by the kernels of ghcm_mlp.cu.
+#pragma once
+
+#include "ghcm_sched.cuh"
+
+namespace ghcm {
+
+// Features of a tile (all roughly in [-1, 1]):
+//   0 (key - front) / span       where the tile's key sits in this wave's key range
+//   1 (kmax - key) / span        spread of the boundary values that activated it
+//   2 never solved
+//   3 (smallest time - key)/span how far the tile's current times lie above the new boundary
+//   4-6 log2 min / max / mean speed / 8
+//   7 active neighbours / 4
+//   8 waves since the tile's last useful solve / 64 (1: never)
+//   9 log2(1 + solves so far) / 8
+//  10 re-queued in full (residual judge or sweep cap)
+//  11 edges with new boundary values / 4
+// key/kmax: the tile's activation keys (float), flags: its scheduler flags.
+__device__ __forceinline__ void tile_features(const Sched& s, uint32_t tile, uint32_t flags, float key, float kmax,
+                                              uint32_t wave, float front, float span, float (&f)[kFeatures]) {
+    const Learn& L = s.learn;
+    float const inv = 1.0f / span;
+    float const k = (key < f_inf()) ? key : front + span;
+    f[0] = fminf(fmaxf((k - front) * inv, 0.f), 1.f);
+    f[1] = fminf(fmaxf((fmaxf(kmax, k) - k) * inv, 0.f), 1.f);
+    float const tm = __ldcg(&s.tmin[tile]);
+    uint32_t const ns = __ldcg(&L.nsolve[tile]);
+    f[2] = ns ? 0.f : 1.f;
+    f[3] = (tm < f_inf()) ? fminf(fmaxf((tm - k) * inv, -1.f), 1.f) : 1.f;
+    float4 const st = __ldg(&L.tstat[tile]);
+    f[4] = st.x;
+    f[5] = st.y;
+    f[6] = st.z;
+    const Inst& I = s.insts[inst_of(s, tile)];
+    uint32_t const local = tile - I.tile_base;
+    uint32_t const tx = local % I.tiles_x, ty = local / I.tiles_x;
+    int act = 0;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        int const nb = neighbour_tile(I, tx, ty, e);
+        if (nb >= 0 && (ld_relaxed(&s.flags[nb]) & kActive)) ++act;
+    }
+    f[7] = 0.25f * static_cast<float>(act);
+    uint32_t const lc = __ldcg(&L.last_change[tile]);
+    f[8] = lc ? fminf(static_cast<float>(wave + 1u - lc), 64.f) * (1.f / 64.f) : 1.f;
+    f[9] = log2f(1.f + static_cast<float>(ns)) * 0.125f;
+    f[10] = (flags & kFull) ? 1.f : 0.f;
+    f[11] = 0.25f * static_cast<float>(__popc((flags & kEdgeMask) >> 4));
+}
+
+// Logit of the MLP for features x, computed by the whole warp (every lane
+// holds x and gets the result). Lane l owns hidden units l and l + 32.
+__device__ __forceinline__ float mlp_logit_warp(const float* __restrict__ P, const float (&x)[kFeatures]) {
+    constexpr unsigned FULL = 0xffffffffu;
+    int const lane = threadIdx.x & 31;
+    float h0 = __ldg(&P[kOffB1 + lane]);
+    float h1 = __ldg(&P[kOffB1 + 32 + lane]);
+#pragma unroll
+    for (int i = 0; i < kFeatures; ++i) {
+        h0 = fmaf(__ldg(&P[kOffW1 + i * kHidden + lane]), x[i], h0);
+        h1 = fmaf(__ldg(&P[kOffW1 + i * kHidden + 32 + lane]), x[i], h1);
+    }
+    h0 = fmaxf(h0, 0.f);
+    h1 = fmaxf(h1, 0.f);
+    float a0 = __ldg(&P[kOffB2 + lane]);
+    float a1 = __ldg(&P[kOffB2 + 32 + lane]);
+#pragma unroll 8
+    for (int k = 0; k < 32; ++k) {
+        float const v = __shfl_sync(FULL, h0, k);
+        a0 = fmaf(__ldg(&P[kOffW2 + k * kHidden + lane]), v, a0);
+        a1 = fmaf(__ldg(&P[kOffW2 + k * kHidden + 32 + lane]), v, a1);
+    }
+#pragma unroll 8
+    for (int k = 0; k < 32; ++k) {
+        float const v = __shfl_sync(FULL, h1, k);
+        a0 = fmaf(__ldg(&P[kOffW2 + (k + 32) * kHidden + lane]), v, a0);
+        a1 = fmaf(__ldg(&P[kOffW2 + (k + 32) * kHidden + 32 + lane]), v, a1);
+    }
+    a0 = fmaxf(a0, 0.f);
+    a1 = fmaxf(a1, 0.f);
+    float z = fmaf(__ldg(&P[kOffW3 + lane]), a0, __ldg(&P[kOffW3 + 32 + lane]) * a1);
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) z += __shfl_xor_sync(FULL, z, o);
+    return z + __ldg(&P[kOffB3]);
+}
+
+// Per-tile log2 speed statistics (features 4-6), one warp per tile.
+template <int B>
+__device__ void tile_speed_stats(const Sched& s, uint32_t tile) {
+    int const lane = threadIdx.x & 31;
+    const Inst& I = s.insts[inst_of(s, tile)];
+    TileCoord const tc = tile_coord<B>(I, tile);
+    float lo = f_inf(), hi = 0.f, sum = 0.f;
+    int n = 0;
+    for (int k = lane; k < B * B; k += 32) {
+        int const lx = k % B, ly = k / B;
+        if (lx >= tc.sx || ly >= tc.sy) continue;
+        float const c = to_cost(I, __ldg(&I.in[static_cast<size_t>(tc.oy + ly) * I.w + tc.ox + lx]));
+        float const v = (c < f_inf() && c > 0.f) ? I.spacing / c : 0.f;  // speed; 0 for walls
+        lo = fminf(lo, v);
+        hi = fmaxf(hi, v);
+        sum += v;
+        ++n;
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        n += __shfl_xor_sync(0xffffffffu, n, o);
+    }
+    if (lane == 0) {
+        auto lg = [](float v) { return fminf(fmaxf(log2f(fmaxf(v, 1e-30f)) * 0.125f, -2.f), 2.f); };
+        s.learn.tstat[tile] = make_float4(lg(lo), lg(hi), lg(sum / static_cast<float>(n > 0 ? n : 1)), 0.f);
+    }
+}
+
+// Score phase: the CTA's warps score the tiles of list[cur][lo, hi) and
+// partition them - taken tiles to s.jobs (up to max_jobs; the overflow is
+// carried), the rest to list[cur ^ 1]. Per round each warp scores one tile;
+// the CTA then reserves its slots with one atomic per list. Carried keys
+// widen s_krange (the key range of list[cur ^ 1]).
+template <int THREADS>
+__device__ void score_phase(const Sched& s, uint32_t cur, uint32_t m, uint32_t wave, uint32_t* s_buf,
+                            uint32_t* s_krange) {
+    constexpr int NW = THREADS / 32;
+    int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    Ctl* ctl = s.ctl;
+    float const front = ld_relaxed_f(&ctl->wave_front);
+    float const span = ld_relaxed_f(&ctl->wave_span);
+    float const thr_logit = logf(s.learn.threshold / (1.f - s.learn.threshold));
+    uint32_t const per = (m + gridDim.x - 1) / gridDim.x;
+    uint32_t const lo = min(m, blockIdx.x * per), hi = min(m, lo + per);
+    // s_buf: [0] take count, [1] carry count, [2] take base, [3] carry base,
+    //        [4, 4+NW) taken tiles, [4+NW, 4+2NW) carried tiles
+    for (uint32_t base = lo; base < hi; base += NW) {
+        if (threadIdx.x < 2) s_buf[threadIdx.x] = 0u;
+        __syncthreads();
+        uint32_t const j = base + static_cast<uint32_t>(warp);
+        if (j < hi) {
+            uint32_t const tile = __ldcg(&s.list[cur][j]);
+            uint32_t const flags = ld_relaxed(&s.flags[tile]);
+            float const key = __uint_as_float(__ldcg(&s.key[tile]));
+            float const kmax = __uint_as_float(__ldcg(&s.learn.kmax[tile]));
+            float x[kFeatures];
+            tile_features(s, tile, flags, key, kmax, wave, front, span, x);
+            float const z = mlp_logit_warp(s.learn.params, x);
+            if (lane == 0) {
+                if ((flags & kFull) || z >= thr_logit) {
+                    s_buf[4 + atomicAdd(&s_buf[0], 1u)] = tile;
+                } else {
+                    s_buf[4 + NW + atomicAdd(&s_buf[1], 1u)] = tile;
+                    uint32_t const kb = __float_as_uint(key < f_inf() ? key : front + span);
+                    atomicMin(&s_krange[0], kb);
+                    atomicMax(&s_krange[1], kb);
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s_buf[2] = s_buf[0] ? atomicAdd(&ctl->take_count, s_buf[0]) : 0u;
+            s_buf[3] = 0u;
+        }
+        __syncthreads();
+        // taken beyond max_jobs are carried too
+        uint32_t const nt = s_buf[0];
+        uint32_t const tbase = s_buf[2];
+        uint32_t const over = (tbase + nt > s.max_jobs) ? min(nt, tbase + nt - s.max_jobs) : 0u;
+        if (threadIdx.x == 0) {
+            uint32_t const nc = s_buf[1] + over;
+            s_buf[3] = nc ? atomicAdd(&ctl->count[cur ^ 1u], nc) : 0u;
+        }
+        __syncthreads();
+        if (threadIdx.x < nt) {
+            uint32_t const t = s_buf[4 + threadIdx.x];
+            uint32_t const pos = tbase + threadIdx.x;
+            if (pos < s.max_jobs) {
+                s.jobs[pos] = t;
+            } else {
+                uint32_t const at = s_buf[3] + s_buf[1] + (pos - max(tbase, s.max_jobs));
+                s.list[cur ^ 1u][at] = t;
+                float const key = __uint_as_float(__ldcg(&s.key[t]));
+                uint32_t const kb = __float_as_uint(key < f_inf() ? key : front + span);
+                atomicMin(&s_krange[0], kb);
+                atomicMax(&s_krange[1], kb);
+            }
+        } else if (threadIdx.x >= 32 && threadIdx.x - 32 < s_buf[1]) {
+            uint32_t const q = threadIdx.x - 32;
+            s.list[cur ^ 1u][s_buf[3] + q] = s_buf[4 + NW + q];
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace ghcm
+
+namespace ghcm {
+
+// Claim-time bookkeeping of a block-solve, by one thread: resets the tile's
+// largest activation key and, when tracing, writes the features the
+// scheduler saw into feat. flags / key_bits: the tile's state as claimed.
+__device__ __forceinline__ uint32_t learn_claim(const Sched& s, uint32_t tile, uint32_t flags, uint32_t key_bits,
+                                                uint32_t wave, float* feat) {
+    if (!s.learn.tstat) return 0u;
+    uint32_t const kmx = atomicExch(&s.learn.kmax[tile], 0u);
+    if (s.learn.trace) {
+        float f[kFeatures];
+        tile_features(s, tile, flags, __uint_as_float(key_bits), __uint_as_float(kmx), wave,
+                      ld_relaxed_f(&s.ctl->wave_front), ld_relaxed_f(&s.ctl->wave_span), f);
+#pragma unroll
+        for (int i = 0; i < kFeatures; ++i) feat[i] = f[i];
+    }
+    return kmx;
+}
+
+// Veto mode: decides, by one whole warp, whether the claimed tile is deferred
+// instead of solved - its score is below the threshold, it was not
+// re-queued in full and it has been deferred fewer than max_vetoes times in a
+// row. Every lane gets the decision.
+__device__ __forceinline__ bool learn_veto_warp(const Sched& s, uint32_t tile, uint32_t flags, uint32_t key_bits,
+                                                uint32_t kmax_bits, uint32_t wave) {
+    if (!s.learn.params || !s.learn.veto || (flags & kFull)) return false;
+    if (__ldcg(&s.learn.vetoes[tile]) >= s.learn.max_vetoes) return false;
+    float x[kFeatures];
+    tile_features(s, tile, flags, __uint_as_float(key_bits), __uint_as_float(kmax_bits), wave,
+                  ld_relaxed_f(&s.ctl->wave_front), ld_relaxed_f(&s.ctl->wave_span), x);
+    float const z = mlp_logit_warp(s.learn.params, x);
+    return z < logf(s.learn.threshold / (1.f - s.learn.threshold));
+}
+
+// A vetoed tile goes back to the next active set with its key, edge bits and
+// largest activation key, by one thread.
+__device__ __forceinline__ void learn_defer(const Sched& s, uint32_t tile, uint32_t flags, uint32_t key_bits,
+                                            uint32_t kmax_bits, uint32_t nxt, uint32_t* s_krange) {
+    __stcg(&s.learn.vetoes[tile], __ldcg(&s.learn.vetoes[tile]) + 1u);
+    atomicMax(&s.learn.kmax[tile], kmax_bits);
+    atomicAdd(&s.ctl->vetoes, 1u);
+    activate(s, tile, flags & (kFull | kEdgeMask), __uint_as_float(key_bits), nxt, s_krange);
+}
+
+// Commit-time bookkeeping, by one thread: solve count, wave of the last
+// useful solve and the trace record.
+__device__ __forceinline__ void learn_commit(const Sched& s, uint32_t tile, bool useful, uint32_t wave,
+                                             uint32_t sweeps, const float* feat) {
+    if (!s.learn.tstat) return;
+    __stcg(&s.learn.nsolve[tile], __ldcg(&s.learn.nsolve[tile]) + 1u);
+    if (s.learn.veto) __stcg(&s.learn.vetoes[tile], 0u);
+    if (useful) __stcg(&s.learn.last_change[tile], wave + 1u);
+    if (s.learn.trace) {
+        uint32_t const pos = atomicAdd(&s.ctl->trace_count, 1u);
+        if (pos < s.learn.trace_cap) {
+            TraceRec& r = s.learn.trace[pos];
+#pragma unroll
+            for (int i = 0; i < kFeatures; ++i) r.f[i] = feat[i];
+            r.tile = tile;
+            r.wave = wave;
+            r.useful = useful ? 1u : 0u;
+            r.sweeps = sweeps;
+        }
+    }
+}
+
+}  // namespace ghcm

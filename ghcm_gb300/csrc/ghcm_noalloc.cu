@@ -73,6 +73,7 @@ extern "C" int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_
     using namespace ghcm;
     int rc = check_config(cfg);
     if (rc != GHCM_OK) return rc;
+    if (cfg->schedule != GHCM_SCHEDULE_PLAIN) return GHCM_ERR_BAD_ARG;  // no model without a context
     if (!d_field || !d_time_out || width == 0 || height == 0 || (n_seeds && !d_seeds_xy)) return GHCM_ERR_BAD_ARG;
     if (!(h > 0.f) || !(h < 3.0e38f)) return GHCM_ERR_BAD_ARG;
     uint32_t const B = cfg->block_size;

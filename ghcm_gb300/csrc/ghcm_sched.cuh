@@ -9,7 +9,14 @@
 namespace ghcm {
 
 // Scheduler phases (Ctl::phase).
-enum : uint32_t { kPhaseInit = 0, kPhaseJobs = 1, kPhaseResidual = 2, kPhaseDone = 3, kPhaseStop = 4 };
+enum : uint32_t {
+    kPhaseInit = 0,
+    kPhaseJobs = 1,      // solve the selected tiles
+    kPhaseResidual = 2,  // global fixed-point check
+    kPhaseDone = 3,
+    kPhaseStop = 4,
+    kPhaseScore = 5,     // learned schedule: score and partition the active set
+};
 
 struct TileCoord {
     uint32_t tx, ty;
@@ -61,9 +68,17 @@ __device__ __forceinline__ float to_cost(const Inst& I, float v) {
 // Puts `tile` into the next active set: lowers its key to `key`, ORs `bits`
 // into its flags and appends it to list[nxt] unless it is already active.
 // The device form of the dirty-set test + heap push + border-mask OR of
-// src/eikonal_hcm.cpp:451-462.
-__device__ __forceinline__ void activate(const Sched& s, uint32_t tile, uint32_t bits, float key, uint32_t nxt) {
-    atomicMin(&s.key[tile], __float_as_uint(key));
+// src/eikonal_hcm.cpp:451-462. s_krange (the calling CTA's {min, max} key
+// bits of what it activated this phase) is widened to `key`.
+__device__ __forceinline__ void activate(const Sched& s, uint32_t tile, uint32_t bits, float key, uint32_t nxt,
+                                         uint32_t* s_krange) {
+    uint32_t const kb = __float_as_uint(key);
+    atomicMin(&s.key[tile], kb);
+    if (s.learn.kmax) atomicMax(&s.learn.kmax[tile], kb);
+    if (s_krange) {
+        atomicMin(&s_krange[0], kb);
+        atomicMax(&s_krange[1], kb);
+    }
     uint32_t const old = atomicOr(&s.flags[tile], kActive | bits);
     if (!(old & kActive)) {
         uint32_t const pos = atomicAdd(&s.ctl->count[nxt], 1u);
@@ -91,43 +106,50 @@ __device__ __forceinline__ uint32_t tile_key(const Sched& s, uint32_t tile) {
 }
 
 // Selects the n smallest keys among the m (> n) tiles of `list`, by the whole
-// CTA: a histogram of SELECT_BINS bins over [min key, max key], a scan for the
-// bin holding the n-th key, then every tile of a lower bin and enough tiles of
-// that bin (in list order) go to s.jobs, the rest to `carry`. The order is
-// exact up to 1/SELECT_BINS of the key range. Returns the number carried.
+// CTA: a histogram of SELECT_BINS bins over [lo, hi] (the keys' range, or a
+// superset of it; with have_range false a first pass finds it), a scan for
+// the bin holding the n-th key, then every tile of a lower bin and enough
+// tiles of that bin (in list order) go to s.jobs, the rest to `carry`. The
+// order is exact up to 1/SELECT_BINS of the range. Returns the number carried.
 constexpr int SELECT_BINS = 2048;
 
 template <int THREADS>
 __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t m, uint32_t n, uint32_t* carry,
-                                 uint32_t* s_hist, uint32_t* s_sel) {
+                                 uint32_t* s_hist, uint32_t* s_sel, float lo, float hi, bool have_range,
+                                 uint32_t jobs_base) {
     __shared__ float s_fmin[THREADS / 32], s_fmax[THREADS / 32];
     int const tid = threadIdx.x;
     int const lane = tid & 31, warp = tid >> 5;
-    // pass 1: range of the finite keys
-    float lo = f_inf(), hi = 0.f;
-    for (uint32_t i = tid; i < m; i += THREADS) {
-        float const k = __uint_as_float(tile_key(s, __ldcg(&list[i])));
-        if (k < f_inf()) {
-            lo = fminf(lo, k);
-            hi = fmaxf(hi, k);
-        }
-    }
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
-        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-    }
-    if (lane == 0) {
-        s_fmin[warp] = lo;
-        s_fmax[warp] = hi;
-    }
     for (int i = tid; i < SELECT_BINS; i += THREADS) s_hist[i] = 0u;
-    __syncthreads();
-    lo = s_fmin[0];
-    hi = s_fmax[0];
-    for (int w = 1; w < THREADS / 32; ++w) {
-        lo = fminf(lo, s_fmin[w]);
-        hi = fmaxf(hi, s_fmax[w]);
+    if (!have_range) {
+        // pass 1: range of the finite keys
+        lo = f_inf();
+        hi = 0.f;
+        for (uint32_t i = tid; i < m; i += THREADS) {
+            float const k = __uint_as_float(tile_key(s, __ldcg(&list[i])));
+            if (k < f_inf()) {
+                lo = fminf(lo, k);
+                hi = fmaxf(hi, k);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        if (lane == 0) {
+            s_fmin[warp] = lo;
+            s_fmax[warp] = hi;
+        }
+        __syncthreads();
+        lo = s_fmin[0];
+        hi = s_fmax[0];
+        for (int w = 1; w < THREADS / 32; ++w) {
+            lo = fminf(lo, s_fmin[w]);
+            hi = fmaxf(hi, s_fmax[w]);
+        }
+    } else {
+        __syncthreads();
     }
     float const span = hi - lo;
     float const scale = (span > 0.f) ? static_cast<float>(SELECT_BINS - 1) / span : 0.f;
@@ -136,9 +158,21 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
         int const b = static_cast<int>((k - lo) * scale);
         return b < 0 ? 0 : (b >= SELECT_BINS ? SELECT_BINS - 1 : b);
     };
-    // pass 2: histogram
-    for (uint32_t i = tid; i < m; i += THREADS)
-        atomicAdd(&s_hist[bin_of(__uint_as_float(tile_key(s, __ldcg(&list[i]))))], 1u);
+    // pass 2: histogram (four keys in flight per thread)
+    {
+        uint32_t i = tid;
+        for (; i + 3u * THREADS < m; i += 4u * THREADS) {
+            uint32_t t4[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) t4[u] = __ldcg(&list[i + u * THREADS]);
+            uint32_t k4[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) k4[u] = tile_key(s, t4[u]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) atomicAdd(&s_hist[bin_of(__uint_as_float(k4[u]))], 1u);
+        }
+        for (; i < m; i += THREADS) atomicAdd(&s_hist[bin_of(__uint_as_float(tile_key(s, __ldcg(&list[i]))))], 1u);
+    }
     __syncthreads();
     // the bin holding the n-th smallest key: thread t scans bins [t*PER, (t+1)*PER)
     constexpr int PER = SELECT_BINS / THREADS;
@@ -184,7 +218,7 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
         bool take = b < bnd;
         if (!take && b == bnd) take = atomicAdd(&s_sel[2], 1u) < take_eq;
         if (take)
-            s.jobs[atomicAdd(&s_sel[3], 1u)] = t;
+            s.jobs[jobs_base + atomicAdd(&s_sel[3], 1u)] = t;
         else
             carry[atomicAdd(&s_sel[4], 1u)] = t;
     }
@@ -228,56 +262,131 @@ __device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned l
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+__device__ __forceinline__ float ld_relaxed_f(const float* p) { return __uint_as_float(ld_relaxed(reinterpret_cast<const uint32_t*>(p))); }
+
+// Runs the plain top-n on list[L] (m tiles): its n lowest keys become jobs
+// base.. of the next JOBS phase (or, with no jobs before them and m <= n, the
+// list itself), the rest is carried to list[L ^ 1], where the activations of
+// that phase also go. Returns {in_list, job count} in s_sel[8], [11].
+template <int THREADS>
+__device__ void plan_plain_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t n, uint32_t base, float lo, float hi,
+                                uint32_t* s_hist, uint32_t* s_sel) {
+    Ctl* ctl = s.ctl;
+    bool const all = m <= n;
+    uint32_t carried = 0u;
+    if (!all) {
+        carried = select_top_n<THREADS>(s, s.list[L], m, n, s.list[L ^ 1u], s_hist, s_sel, lo, hi, s.key_mode == 0u,
+                                        base);
+    } else if (base) {
+        for (uint32_t i = threadIdx.x; i < m; i += THREADS) s.jobs[base + i] = __ldcg(&s.list[L][i]);
+    }
+    if (threadIdx.x == 0) {
+        ctl->count[L ^ 1u] = carried;
+        // the carried keys lie in [lo, hi]: a superset range for list[L ^ 1]
+        ctl->krange[L ^ 1u][0] = carried ? __float_as_uint(lo) : inf_bits();
+        ctl->krange[L ^ 1u][1] = carried ? __float_as_uint(hi) : 0u;
+        s_sel[8] = (all && base == 0u) ? 1u : 0u;
+        s_sel[11] = base + (all ? m : m - carried);
+    }
+}
+
 // Decides the next phase; run by the whole of the last CTA to reach the wave
 // barrier while every other CTA waits. `st` is this CTA's view of the state
 // the previous barrier published. Returns the new
 // {jobs-in-list, phase, cur, job count} in s_sel[8..11].
 //   after INIT / JOBS / RESIDUAL, the set to process is list[act]:
-//     non-empty          -> JOBS on its n lowest keys (the rest carried over)
-//     empty after JOBS   -> RESIDUAL: the global fixed-point check
-//     empty after RESID. -> DONE
+//     non-empty, plain        -> JOBS on its n lowest keys (the rest carried over)
+//     non-empty, learned      -> SCORE: partition it by the model's score
+//     empty after JOBS        -> RESIDUAL: the global fixed-point check
+//     empty after RESIDUAL    -> DONE
+//   after SCORE: JOBS on the tiles it took, filled up to fallback_jobs from
+//   the carried set in plain key order (all of the wave when it took none).
+// The key range of list[act] comes from the activations (ctl->krange); its
+// min and span are published as this wave's front for the features.
 template <int THREADS>
 __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_hist, uint32_t* s_sel) {
     Ctl* ctl = s.ctl;
     int const tid = threadIdx.x;
     uint32_t const prev = st[kStPhase];
     uint32_t const cur = st[kStCur];
-    uint32_t const act = (prev == kPhaseInit) ? 0u : (cur ^ 1u);
-    uint32_t const m = ld_relaxed(&ctl->count[act]);
-    uint32_t phase, ncur = cur, jobs = 0u, in_list = 0u;
-    if (m == 0u) {
-        if (prev == kPhaseResidual) {
-            phase = kPhaseDone;
-        } else {
-            phase = kPhaseResidual;
-            ncur = act ^ 1u;  // residual activations go to list[act], now empty
+    uint32_t phase = kPhaseJobs, ncur = cur;
+    if (prev == kPhaseScore) {
+        // the score phase took `take` tiles into jobs[0, take) and carried the
+        // rest to list[L]; fill the wave up to fallback_jobs from list[L] in
+        // plain key order
+        uint32_t const L = cur ^ 1u;
+        uint32_t const take = min(ld_relaxed(&ctl->take_count), s.max_jobs);
+        uint32_t const want = min(s.learn.fallback_jobs, s.max_jobs);
+        uint32_t const m = ld_relaxed(&ctl->count[L]);
+        if (take >= want || m == 0u) {
             if (tid == 0) {
-                ctl->count[act] = 0u;
-                atomicAdd(&ctl->residual_passes, 1u);
+                s_sel[8] = 0u;
+                s_sel[11] = take;
+                atomicAdd(&ctl->score_waves, 1u);
             }
+        } else {
+            float const lo = __uint_as_float(ld_relaxed(&ctl->krange[L][0]));
+            float const hi = __uint_as_float(ld_relaxed(&ctl->krange[L][1]));
+            plan_plain_jobs<THREADS>(s, L, m, want - take, take, lo, hi, s_hist, s_sel);
+            ncur = L;
+            if (tid == 0) atomicAdd(take ? &ctl->score_waves : &ctl->fallback_waves, 1u);
         }
-    } else if (s.max_waves != 0u && st[kStWaves] >= s.max_waves) {
-        phase = kPhaseStop;
-        if (tid == 0) atomicOr(&ctl->error, kErrNotConverged);
+        if (tid == 0) atomicAdd(&ctl->waves, 1u);
     } else {
-        uint32_t carried = 0u;
-        bool const all = m <= s.max_jobs;
-        if (!all) carried = select_top_n<THREADS>(s, s.list[act], m, s.max_jobs, s.list[act ^ 1u], s_hist, s_sel);
-        phase = kPhaseJobs;
-        ncur = act;
-        jobs = all ? m : m - carried;
-        in_list = all ? 1u : 0u;
-        if (tid == 0) {
-            ctl->count[act ^ 1u] = carried;
-            atomicAdd(&ctl->waves, 1u);
-            atomicMax(&ctl->max_active, m);
+        uint32_t const act = (prev == kPhaseInit) ? 0u : (cur ^ 1u);
+        uint32_t const m = ld_relaxed(&ctl->count[act]);
+        if (m == 0u) {
+            if (prev == kPhaseResidual) {
+                phase = kPhaseDone;
+            } else {
+                phase = kPhaseResidual;
+                ncur = act ^ 1u;  // residual activations go to list[act], now empty
+                if (tid == 0) {
+                    ctl->count[act] = 0u;
+                    ctl->krange[act][0] = inf_bits();
+                    ctl->krange[act][1] = 0u;
+                    atomicAdd(&ctl->residual_passes, 1u);
+                }
+            }
+            if (tid == 0) {
+                s_sel[8] = 0u;
+                s_sel[11] = 0u;
+            }
+        } else if (s.max_waves != 0u && st[kStWaves] >= s.max_waves) {
+            phase = kPhaseStop;
+            if (tid == 0) {
+                atomicOr(&ctl->error, kErrNotConverged);
+                s_sel[8] = 0u;
+                s_sel[11] = 0u;
+            }
+        } else {
+            float const lo = __uint_as_float(ld_relaxed(&ctl->krange[act][0]));
+            float const hi = __uint_as_float(ld_relaxed(&ctl->krange[act][1]));
+            if (tid == 0) {
+                ctl->wave_front = (lo < f_inf()) ? lo : 0.f;
+                ctl->wave_span = (hi > lo && lo < f_inf()) ? hi - lo : 1.f;
+                atomicMax(&ctl->max_active, m);
+            }
+            ncur = act;
+            if (s.learn.params && !s.learn.veto) {
+                phase = kPhaseScore;  // carries and activations go to list[act ^ 1]
+                if (tid == 0) {
+                    ctl->count[act ^ 1u] = 0u;
+                    ctl->krange[act ^ 1u][0] = inf_bits();
+                    ctl->krange[act ^ 1u][1] = 0u;
+                    ctl->take_count = 0u;
+                    s_sel[8] = 1u;
+                    s_sel[11] = m;  // tiles to score
+                }
+            } else {
+                plan_plain_jobs<THREADS>(s, act, m, s.max_jobs, 0u, lo, hi, s_hist, s_sel);
+                if (tid == 0) atomicAdd(&ctl->waves, 1u);
+            }
         }
     }
     if (tid == 0) {
-        s_sel[8] = in_list;
         s_sel[9] = phase;
         s_sel[10] = ncur;
-        s_sel[11] = jobs;
     }
 }
 
@@ -287,11 +396,21 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
 // waits are bounded. On return s_state holds the new state; returns false
 // when the grid must stop (timeout or error).
 template <int THREADS>
-__device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, uint32_t* s_state) {
+__device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, uint32_t* s_state,
+                             uint32_t* s_krange) {
     __shared__ uint32_t s_last;
     Ctl* ctl = s.ctl;
     __syncthreads();
     if (threadIdx.x == 0) {
+        // the keys this CTA activated or carried in the phase just run went
+        // to list[cur ^ 1]: fold their range into that list's
+        if (s_krange[0] <= s_krange[1]) {
+            uint32_t const nxt = s_state[kStCur] ^ 1u;
+            atomicMin(&ctl->krange[nxt][0], s_krange[0]);
+            atomicMax(&ctl->krange[nxt][1], s_krange[1]);
+        }
+        s_krange[0] = inf_bits();
+        s_krange[1] = 0u;
         __threadfence();  // publish this CTA's work
         uint32_t const arrived = atomicAdd(&ctl->bar_count, 1u) + 1u;
         s_last = (arrived == gridDim.x) ? 1u : 0u;

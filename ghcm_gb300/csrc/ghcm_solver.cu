@@ -52,7 +52,7 @@ constexpr int max_ctas_per_sm() {
 }
 
 template <int B, bool FIM>
-__global__ void __launch_bounds__(TileGeom<B>::THREADS) k_solve(const __grid_constant__ Sched s) {
+__global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_solve(const __grid_constant__ Sched s) {
     using G = TileGeom<B>;
     __shared__ TileSmem<B> sm;
     __shared__ __align__(8) uint64_t s_bar;
@@ -61,6 +61,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS) k_solve(const __grid_con
     __shared__ uint32_t s_state[8];
     __shared__ uint32_t s_word[8];
     __shared__ float s_red[G::THREADS / 32];
+    __shared__ uint32_t s_krange[2];
     int const tid = threadIdx.x;
     Ctl* ctl = s.ctl;
     if (ld_relaxed(&ctl->error) != 0u) return;  // the init kernels rejected the input
@@ -69,6 +70,10 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS) k_solve(const __grid_con
     if (FIM)
         for (int i = tid; i < B * B; i += G::THREADS) sm.check[i] = 0;
     if (tid < 8) s_state[tid] = 0u;  // INIT, generation 0, no waves yet
+    if (tid == 0) {
+        s_krange[0] = inf_bits();  // keys this CTA activates in a phase: {min, max}
+        s_krange[1] = 0u;
+    }
     __syncthreads();
     GHCM_PROF_BEGIN(t_kernel);
     uint32_t parity = 0u;
@@ -79,7 +84,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS) k_solve(const __grid_con
     uint32_t const nwarps = gridDim.x * warps_per_cta;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
-        bool const ok = wave_barrier<G::THREADS>(s, s_hist, s_sel, s_state);
+        bool const ok = wave_barrier<G::THREADS>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
         uint32_t const phase = s_state[kStPhase];
@@ -87,16 +92,20 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS) k_solve(const __grid_con
         if (phase == kPhaseJobs) {
             GHCM_PROF_BEGIN(t_solve);
             uint32_t const nj = s_state[kStJobs];
+            uint32_t const wave = s_state[kStWaves];
             const uint32_t* jobs = s_state[kStInList] ? s.list[cur] : s.jobs;
             for (uint32_t j = blockIdx.x; j < nj; j += gridDim.x) {
-                if (!solve_tile<B, FIM>(s, __ldcg(&jobs[j]), cur ^ 1u, sm, &s_bar, parity, tma_pending, s_word, s_red))
-                    break;
-                ++solves;
+                int const r = solve_tile<B, FIM>(s, __ldcg(&jobs[j]), cur ^ 1u, sm, &s_bar, parity, tma_pending,
+                                                 s_word, s_red, s_krange, wave);
+                if (r == kJobFailed) break;
+                solves += (r == kJobSolved) ? 1u : 0u;
             }
             GHCM_PROF_END(ctl, 1, t_solve);
+        } else if (phase == kPhaseScore) {
+            score_phase<G::THREADS>(s, cur, s_state[kStJobs], s_state[kStWaves] + 1u, s_hist, s_krange);
         } else if (phase == kPhaseResidual) {
             GHCM_PROF_BEGIN(t_res);
-            residual_warp<B>(s, cur ^ 1u, gw, nwarps);
+            residual_warp<B>(s, cur ^ 1u, gw, nwarps, s_krange);
             GHCM_PROF_END(ctl, 4, t_res);
         } else {
             break;  // done or stopped
@@ -119,6 +128,7 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
     __shared__ uint32_t s_hist[SELECT_BINS];
     __shared__ uint32_t s_sel[16];
     __shared__ uint32_t s_state[8];
+    __shared__ uint32_t s_krange[2];
     int const tid = threadIdx.x;
     int const warp = tid >> 5;
     int const lane = tid & 31;
@@ -128,6 +138,10 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
 
     if (lane == 0) mbar_init(&sm.bar, 1);
     if (tid < 8) s_state[tid] = 0u;  // INIT, generation 0, no waves yet
+    if (tid == 0) {
+        s_krange[0] = inf_bits();
+        s_krange[1] = 0u;
+    }
     __syncthreads();
     GHCM_PROF_BEGIN(t_kernel);
     uint32_t parity = 0u;
@@ -137,7 +151,7 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
     uint32_t const nwarps = gridDim.x * W::NW;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
-        bool const ok = wave_barrier<W::THREADS>(s, s_hist, s_sel, s_state);
+        bool const ok = wave_barrier<W::THREADS>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
         uint32_t const phase = s_state[kStPhase];
@@ -145,15 +159,19 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
         if (phase == kPhaseJobs) {
             GHCM_PROF_BEGIN(t_solve);
             uint32_t const nj = s_state[kStJobs];
+            uint32_t const wave = s_state[kStWaves];
             const uint32_t* jobs = s_state[kStInList] ? s.list[cur] : s.jobs;
             for (uint32_t j = gw; j < nj; j += nwarps) {
-                if (!solve_tile_warp<B>(s, __ldcg(&jobs[j]), cur ^ 1u, sm, parity, tma_pending)) break;
-                ++solves;
+                int const r = solve_tile_warp<B>(s, __ldcg(&jobs[j]), cur ^ 1u, sm, parity, tma_pending, s_krange, wave);
+                if (r == kJobFailed) break;
+                solves += (r == kJobSolved) ? 1u : 0u;
             }
             GHCM_PROF_END(ctl, 1, t_solve);
+        } else if (phase == kPhaseScore) {
+            score_phase<W::THREADS>(s, cur, s_state[kStJobs], s_state[kStWaves] + 1u, s_hist, s_krange);
         } else if (phase == kPhaseResidual) {
             GHCM_PROF_BEGIN(t_res);
-            residual_warp<B>(s, cur ^ 1u, gw, nwarps);
+            residual_warp<B>(s, cur ^ 1u, gw, nwarps, s_krange);
             GHCM_PROF_END(ctl, 4, t_res);
         } else {
             break;  // done or stopped
@@ -184,6 +202,12 @@ __global__ void k_init_inst(Sched s) {
         s.key[g] = inf_bits();
         s.tmin[g] = f_inf();
         if (s.tile_inst) const_cast<uint32_t*>(s.tile_inst)[g] = blockIdx.y;
+        if (s.learn.tstat) {
+            s.learn.kmax[g] = 0u;
+            s.learn.nsolve[g] = 0u;
+            s.learn.last_change[g] = 0u;
+            s.learn.vetoes[g] = 0u;
+        }
     }
     size_t const n = static_cast<size_t>(I.w) * I.h;
     bool bad = false;
@@ -213,9 +237,17 @@ __global__ void k_init_seeds(Sched s, int block) {
             if (px < 0 || py < 0 || px >= static_cast<int>(I.w) || py >= static_cast<int>(I.h)) continue;
             uint32_t const tile = I.tile_base + static_cast<uint32_t>(py / block) * I.tiles_x + px / block;
             s.tmin[tile] = 0.f;
-            activate(s, tile, 0u, 0.f, 0u);
+            activate(s, tile, 0u, 0.f, 0u, nullptr);  // key range of list 0: {0, 0} from the zeroed Ctl
         }
     }
+}
+
+// Per-tile speed statistics for the learned features, one warp per tile.
+template <int B>
+__global__ void k_tile_stats(Sched s) {
+    uint32_t const warps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t t = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); t < s.num_tiles; t += warps)
+        tile_speed_stats<B>(s, t);
 }
 
 __global__ void k_wait_selftest(const uint32_t* flag, Ctl* ctl, uint64_t timeout_ns) {
@@ -301,6 +333,14 @@ cudaError_t launch_init(const Sched& s, uint32_t n_insts, uint64_t max_cells, ui
     unsigned const per = static_cast<unsigned>(std::max<uint64_t>(8u, 152u * 16u * 4u / n_insts));
     unsigned const gx = static_cast<unsigned>(std::max<uint64_t>(1u, std::min<uint64_t>(want, per)));
     k_init_inst<<<dim3(gx, n_insts), tb, 0, st>>>(s);
+    if (s.learn.tstat) {
+        unsigned const g = static_cast<unsigned>(std::min<uint32_t>((s.num_tiles + 7u) / 8u, 152u * 16u));
+        switch (block) {
+            case 8: k_tile_stats<8><<<g, tb, 0, st>>>(s); break;
+            case 16: k_tile_stats<16><<<g, tb, 0, st>>>(s); break;
+            default: k_tile_stats<32><<<g, tb, 0, st>>>(s); break;
+        }
+    }
     if (max_seeds) {
         unsigned const sb = 128;
         unsigned const gs = std::min<unsigned>((max_seeds + sb - 1) / sb, 64u);

@@ -28,7 +28,7 @@
 // the second condition two converged tiles can keep activating each other.
 #pragma once
 
-#include "ghcm_sched.cuh"
+#include "ghcm_learn.cuh"
 
 namespace ghcm {
 
@@ -52,6 +52,7 @@ struct alignas(128) TileSmem {
     float time[TileGeom<B>::BOXP];
     float cost[TileGeom<B>::BOXP];
     uint8_t check[B * B];  // block-FIM: re-check requests
+    float feat[kFeatures]; // trace recorder: features of the current solve
 };
 
 // index of local cell (x, y), x in [-4, B+4), y in [-2, B+2), in a staged box
@@ -60,11 +61,17 @@ __device__ __forceinline__ int si(int x, int y) {
     return (y + 2) * TileGeom<B>::BW + x + 4;
 }
 
-// One block-solve of `tile`; activations go to list[nxt]. Returns false if
-// the TMA stage timed out (the grid then stops at the next barrier).
+// Outcome of a claimed job.
+enum : int { kJobFailed = 0, kJobSolved = 1, kJobDeferred = 2 };
+
+// One block-solve of `tile`; activations go to list[nxt]. Returns kJobSolved,
+// kJobDeferred (the learned schedule's veto put it back in the active set) or
+// kJobFailed if the TMA stage timed out (the grid then stops at the next
+// barrier).
 template <int B, bool FIM>
-__device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<B>& sm, uint64_t* bar,
-                           uint32_t& parity, bool& tma_pending, uint32_t* s_word, float* s_red) {
+__device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<B>& sm, uint64_t* bar,
+                           uint32_t& parity, bool& tma_pending, uint32_t* s_word, float* s_red, uint32_t* s_krange,
+                           uint32_t wave) {
     using G = TileGeom<B>;
     int const tid = threadIdx.x;
     uint32_t const ii = inst_of(s, tile);
@@ -76,11 +83,14 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
     // it), then stage the tile with its halo.
     if (tid == 0) {
         uint32_t const f = atomicAnd(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
-        atomicExch(&s.key[tile], inf_bits());
+        uint32_t const kold = atomicExch(&s.key[tile], inf_bits());
+        uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
         __threadfence();
         s_word[0] = f;
         s_word[1] = 0u;  // abort flag
         s_word[4] = 0u;  // edge rows changed by this solve
+        s_word[5] = kold;
+        s_word[6] = kmx;
         if (use_tma) {
             fence_proxy_async();
             mbar_arrive_expect_tx(bar, static_cast<uint32_t>(2 * G::BOX * sizeof(float)));
@@ -91,6 +101,16 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
     }
     __syncthreads();
     uint32_t const flags = s_word[0];
+    // learned schedule, veto mode: warp 0 scores the tile while its stage is in flight
+    bool const may_veto = s.learn.veto && s.learn.params;
+    if (may_veto) {
+        if (tid < 32) {
+            bool const v = learn_veto_warp(s, tile, flags, s_word[5], s_word[6], wave);
+            if (tid == 0) s_word[7] = v ? 1u : 0u;
+        }
+        __syncthreads();
+    }
+    bool const vetoed = may_veto && s_word[7] != 0u;
     if (use_tma) {
         if (!mbar_wait(bar, parity, s.timeout_ns)) {
             atomicOr(&s.ctl->error, kErrTimeout);
@@ -99,6 +119,13 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
             tma_pending = false;
         }
         parity ^= 1u;
+    }
+    if (vetoed) {
+        __syncthreads();
+        if (s_word[1]) return kJobFailed;
+        if (tid == 0) learn_defer(s, tile, flags, s_word[5], s_word[6], nxt, s_krange);
+        __syncthreads();
+        return kJobDeferred;
     }
     // fill / fix up the two rings: outside the field is +inf; speed -> cost
     for (int r = tid; r < G::RING; r += G::THREADS) {
@@ -118,7 +145,7 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
         }
     }
     __syncthreads();
-    if (s_word[1]) return false;
+    if (s_word[1]) return kJobFailed;
 
     constexpr int BW = G::BW;
     float t[G::CPT], t0[G::CPT], c[G::CPT], c2[G::CPT];
@@ -292,6 +319,13 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
 
     // Commit the tile and its smallest time.
     bool const tile_changed = __syncthreads_or(own_changed) != 0;
+    bool useful = false;  // some cell moved by more than eps (the trace label)
+    if (s.learn.tstat) {
+        bool mv = false;
+#pragma unroll
+        for (int k = 0; k < G::CPT; ++k) mv |= inside[k] && time_diff(t[k], t0[k]) < -eps;
+        useful = __syncthreads_or(mv) != 0;
+    }
     float lmin = f_inf();
 #pragma unroll
     for (int k = 0; k < G::CPT; ++k) {
@@ -310,15 +344,16 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
         float m = s_red[0];
         for (int w = 1; w < G::THREADS / 32; ++w) m = fminf(m, s_red[w]);
         s.tmin[tile] = m;
+        learn_commit(s, tile, useful, wave, sweeps, sm.feat);
         if (capped) {
             __threadfence();
-            activate(s, tile, kFull, m, nxt);
+            activate(s, tile, kFull, m, nxt, s_krange);
         }
     }
     uint32_t const edge_changed = s_word[4];
     if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u)) {
         __threadfence();
-        activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt);
+        activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt, s_krange);
     }
 #ifdef GHCM_PROFILE
     if (tid == 0) {
@@ -327,14 +362,14 @@ __device__ bool solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem
     }
 #endif
     __syncthreads();
-    return true;
+    return kJobSolved;
 }
 
 // Global residual judge, one tile per warp: re-activates every tile holding
 // a cell whose Godunov update would still lower it by more than eps. The
 // reference has no such check (src/eikonal_hcm.cpp:343, 486-488).
 template <int B>
-__device__ void residual_warp(const Sched& s, uint32_t nxt, uint32_t warp_global, uint32_t warps) {
+__device__ void residual_warp(const Sched& s, uint32_t nxt, uint32_t warp_global, uint32_t warps, uint32_t* s_krange) {
     int const lane = threadIdx.x & 31;
     for (uint32_t tile = warp_global; tile < s.num_tiles; tile += warps) {
         const Inst& I = s.insts[inst_of(s, tile)];
@@ -362,7 +397,7 @@ __device__ void residual_warp(const Sched& s, uint32_t nxt, uint32_t warp_global
         if (__any_sync(0xffffffffu, bad)) {
 #pragma unroll
             for (int o = 16; o >= 1; o >>= 1) kmin = fminf(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
-            if (lane == 0) activate(s, tile, kFull, kmin, nxt);
+            if (lane == 0) activate(s, tile, kFull, kmin, nxt, s_krange);
         }
     }
 }

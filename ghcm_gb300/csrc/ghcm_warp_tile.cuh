@@ -32,14 +32,17 @@ template <int B>
 struct alignas(128) WarpTileSmem {
     float time[TileGeom<B>::BOXP];
     float cost[TileGeom<B>::BOXP];
+    float feat[kFeatures];
+    uint32_t claim[4];  // flags, key, largest activation key of the claimed tile
     uint64_t bar;
 };
 
-// One block-solve of `tile` by the calling warp. Returns false if the TMA stage
-// timed out.
+// One block-solve of `tile` by the calling warp. Returns kJobSolved,
+// kJobDeferred (vetoed by the learned schedule) or kJobFailed (the TMA stage
+// timed out).
 template <int B>
-__device__ bool solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, WarpTileSmem<B>& sm, uint32_t& parity,
-                                bool& tma_pending) {
+__device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, WarpTileSmem<B>& sm, uint32_t& parity,
+                                bool& tma_pending, uint32_t* s_krange, uint32_t wave) {
     using G = TileGeom<B>;
     using W = WarpTileGeom<B>;
     constexpr unsigned FULL = 0xffffffffu;
@@ -54,8 +57,12 @@ __device__ bool solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, War
 
     // Claim and stage.
     if (lane == 0) {
-        atomicAnd(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
-        atomicExch(&s.key[tile], inf_bits());
+        uint32_t const f = atomicAnd(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
+        uint32_t const kold = atomicExch(&s.key[tile], inf_bits());
+        uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
+        sm.claim[0] = f;
+        sm.claim[1] = kold;
+        sm.claim[2] = kmx;
         __threadfence();
         if (use_tma) {
             fence_proxy_async();
@@ -66,14 +73,20 @@ __device__ bool solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, War
         }
     }
     __syncwarp();
+    bool const vetoed = learn_veto_warp(s, tile, sm.claim[0], sm.claim[1], sm.claim[2], wave);
     if (use_tma) {
         bool const landed = mbar_wait(&sm.bar, parity, s.timeout_ns);
         parity ^= 1u;
         if (!__all_sync(FULL, landed)) {
             if (lane == 0) atomicOr(&s.ctl->error, kErrTimeout);
-            return false;
+            return kJobFailed;
         }
         if (lane == 0) tma_pending = false;
+    }
+    if (vetoed) {
+        if (lane == 0) learn_defer(s, tile, sm.claim[0], sm.claim[1], sm.claim[2], nxt, s_krange);
+        __syncwarp();
+        return kJobDeferred;
     }
     for (int r = lane; r < G::RING; r += 32) {
         int const lx = r % (B + 4) - 2, ly = r / (B + 4) - 2;
@@ -139,11 +152,13 @@ __device__ bool solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, War
     // The converged tile into the box interior (for the probes), noting the
     // edge rows this solve changed against the staged values it replaces.
     uint32_t ec = 0u;
+    bool mv = false;  // some cell moved by more than eps
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         int const y = band * R + k;
         float const staged = sm.time[si<B>(x, y)];
         sm.time[si<B>(x, y)] = t[k];
+        mv |= x < tc.sx && y < tc.sy && time_diff(t[k], staged) < -eps;
         if (x < tc.sx && y < tc.sy && t[k] != staged) {
             if (x == 0) ec |= 1u;
             if (y == 0) ec |= 2u;
@@ -204,6 +219,7 @@ __device__ bool solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, War
 
     // Commit (coalesced along rows) and the smallest time.
     bool const tile_changed = __any_sync(FULL, changed);
+    bool const useful = __any_sync(FULL, mv);  // the trace label
     float lmin = f_inf();
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -220,19 +236,20 @@ __device__ bool solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, War
     if (lane == 0) {
         __threadfence();  // the warp's tile stores before its activations
         s.tmin[tile] = lmin;
+        learn_commit(s, tile, useful, wave, sweeps, sm.feat);
 #pragma unroll
         for (int e = 0; e < 4; ++e)
             if (((imp_mask & ec) >> e) & 1u)
                 activate(s, static_cast<uint32_t>(neighbour_tile(I, tc.tx, tc.ty, e)), kEdgeBit0 << ((e + 2) & 3),
-                         keys[e], nxt);
-        if (capped) activate(s, tile, kFull, lmin, nxt);
+                         keys[e], nxt, s_krange);
+        if (capped) activate(s, tile, kFull, lmin, nxt, s_krange);
 #ifdef GHCM_PROFILE
         atomicAdd(&s.ctl->prof[3], static_cast<unsigned long long>(sweeps));
         atomicMax(&s.ctl->wave_max_sweeps, sweeps);
 #endif
     }
     __syncwarp();
-    return true;
+    return kJobSolved;
 }
 
 }  // namespace ghcm

@@ -67,6 +67,7 @@ class HcmConfig:
     wait_timeout_ms: int = 2000
     use_tma: bool = True
     device: int = -1
+    fallback_jobs: int = 0                 # learned schedule: n of a wave in which no tile qualifies
 
     def to_c(self, sm_count: int | None = None) -> GhcmConfig:
         c = GhcmConfig()
@@ -85,6 +86,7 @@ class HcmConfig:
         c.wait_timeout_ms = int(self.wait_timeout_ms)
         c.device = int(self.device)
         c.use_tma = 1 if self.use_tma else 0
+        c.fallback_jobs = int(self.fallback_jobs)
         return c
 
 

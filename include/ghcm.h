@@ -68,7 +68,9 @@ typedef struct ghcm_config {
     uint32_t wait_timeout_ms; /* limit of every device-side wait; 0 = 2000 */
     int32_t  device;          /* CUDA device ordinal; -1 = the current device */
     uint32_t use_tma;         /* 1 = stage tiles with TMA when the field allows it; 0 = plain loads */
-    uint32_t reserved[5];     /* must be zero */
+    uint32_t fallback_jobs;   /* learned schedule: n of the plain top-n of a wave in which no tile
+                                 qualifies; 0 = max_jobs */
+    uint32_t reserved[4];     /* must be zero */
 } ghcm_config;
 
 typedef struct ghcm_stats {
@@ -192,6 +194,97 @@ int ghcm_autotune_batch(const ghcm_config* base, const ghcm_instance* insts, uin
                         uint32_t reps, ghcm_config* best, ghcm_tune_trial* trials, uint32_t max_trials,
                         uint32_t* n_trials);
 
+/* ---- learned block schedule ----
+ * No counterpart in the reference, whose only order is the min-time priority
+ * queue (src/eikonal_hcm.cpp:47-80, 344-358). A 12 -> 64 -> 64 -> 1 FP32 MLP
+ * (ReLU, sigmoid output) scores each active tile with P(its solve moves some
+ * cell by more than eps). With cfg.schedule = GHCM_SCHEDULE_LEARNED and a
+ * model set, every wave solves the tiles scoring >= threshold (plus tiles
+ * re-queued by the residual judge or a sweep cap), up to cfg.max_jobs; a wave
+ * in which none qualifies falls back to the plain top-n. The global Godunov
+ * residual check still decides convergence.
+ *
+ * Features (in this order, each roughly in [-1, 1]): the tile's key relative
+ * to the wave's key range; the spread of its activation keys; never solved;
+ * its smallest time above its key; log2 min / max / mean speed / 8; active
+ * neighbours / 4; waves since its last useful solve / 64; log2(1 + solves) / 8;
+ * re-queued in full; edges with new boundary values / 4.
+ *
+ * Parameters, flat float32 (GHCM_MLP_PARAMS): W1[12][64] (input-major), b1[64],
+ * W2[64][64] (input-major), b2[64], W3[64], b3. */
+#define GHCM_MLP_FEATURES 12
+#define GHCM_MLP_HIDDEN   64
+#define GHCM_MLP_PARAMS   5057
+
+/* One block-solve of a trace: the features of the tile when the solve was
+ * scheduled and whether it moved some cell by more than eps. */
+typedef struct ghcm_trace_record {
+    float    features[GHCM_MLP_FEATURES];
+    uint32_t tile;
+    uint32_t wave;
+    uint32_t useful;    /* 1: some cell moved by more than eps */
+    uint32_t sweeps;    /* inner sweeps of the solve */
+} ghcm_trace_record;
+
+/* Records a trace of every block-solve of the following solves on ctx, up to
+ * `capacity` records per solve (0 turns tracing off). */
+int ghcm_trace_enable(ghcm_ctx* ctx, uint32_t capacity);
+
+/* Copies the last solve's trace: up to max_records to out; *n_records = how
+ * many were copied, *n_total (optional) = solves the trace saw (more than the
+ * capacity when it overflowed). */
+int ghcm_trace_read(ghcm_ctx* ctx, ghcm_trace_record* out, uint32_t max_records, uint32_t* n_records,
+                    uint32_t* n_total);
+
+/* Sets the model of the learned schedule (host parameters, copied) and its
+ * threshold in (0, 1). NULL params clear it. */
+int ghcm_set_schedule_model(ghcm_ctx* ctx, const float* params, uint32_t n_params, float threshold);
+
+/* How the learned schedule uses the model:
+ *   GHCM_POLICY_SCORE (default): a score phase before every wave scores the whole active
+ *     set; the wave solves the tiles at or above the threshold, filled up to
+ *     cfg.fallback_jobs tiles in plain key order.
+ *   GHCM_POLICY_VETO: the plain top-n proposes the wave; a CTA that
+ *     claims a tile scores it first and defers it (back into the active set,
+ *     key and edge bits kept) when the score is below the threshold, at most
+ *     max_vetoes times in a row per tile (0 = 2). */
+#define GHCM_POLICY_SCORE 0
+#define GHCM_POLICY_VETO  1
+int ghcm_set_schedule_policy(ghcm_ctx* ctx, uint32_t policy, uint32_t max_vetoes);
+
+/* Learned-schedule counters of the last solve on ctx: out[0] waves chosen by
+ * score, out[1] waves that fell back to the plain top-n, out[2] trace
+ * records seen, out[3] claims deferred by a veto. */
+int ghcm_schedule_counters(const ghcm_ctx* ctx, uint32_t out[4]);
+
+/* Inference kernel: d_prob[i] = sigmoid(MLP(d_x[i*12 .. i*12+12))) on the
+ * device, on `stream`; asynchronous. */
+int ghcm_mlp_forward(const float* d_params, const float* d_x, uint32_t n, float* d_prob, void* stream);
+
+/* Gradient kernel: adds the gradient of the summed weighted BCE loss of
+ * samples (d_x, d_y in {0, 1}) to d_grad (GHCM_MLP_PARAMS floats) and the
+ * summed loss to *d_loss_sum; asynchronous. */
+int ghcm_mlp_grad(const float* d_params, const float* d_x, const float* d_y, uint32_t n, float pos_weight,
+                  float* d_grad, float* d_loss_sum, void* stream);
+
+typedef struct ghcm_train_config {
+    uint32_t epochs;
+    uint32_t batch;           /* samples per Adam step */
+    float    lr;
+    float    beta1, beta2, adam_eps;
+    float    pos_weight;      /* weight of the positive (useful) class in the loss */
+    uint32_t reserved[5];     /* must be zero */
+} ghcm_train_config;
+
+int ghcm_train_config_default(ghcm_train_config* cfg);
+
+/* Trains the parameters in place (d_params, device) on n samples with Adam,
+ * mini-batches taken in order (shuffle the samples beforehand). Blocks until
+ * done. epoch_losses (optional, host, cfg->epochs floats) receives the mean
+ * loss of each epoch. */
+int ghcm_mlp_train(const float* d_x, const float* d_y, uint32_t n, float* d_params, const ghcm_train_config* cfg,
+                   void* stream, float* epoch_losses);
+
 /* Number of SMs of the context's device (the reference's compute units). */
 int ghcm_device_sm_count(const ghcm_ctx* ctx, uint32_t* out);
 
@@ -218,7 +311,8 @@ int ghcm_abi_version(void);
  * All calls share the one scratch array: calls that overlap on the GPU (other
  * streams or host threads) race and must be serialised by the caller. The
  * first call on a device looks up the array's device address; make it before
- * capturing a stream into a CUDA graph. No statistics are returned. */
+ * capturing a stream into a CUDA graph. No statistics are returned. Plain
+ * schedule only (cfg->schedule must be GHCM_SCHEDULE_PLAIN). */
 int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_field, int input_is_speed, uint32_t width,
                               uint32_t height, float h, const uint32_t* d_seeds_xy, uint32_t n_seeds,
                               float* d_time_out, void* stream);

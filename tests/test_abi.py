@@ -38,10 +38,11 @@ def test_struct_layouts_match_c(tmp_path):
     src = tmp_path / "sizes.c"
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "ghcm.h"\n'
-        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(ghcm_config), sizeof(ghcm_stats),"
+        "int main(void){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(ghcm_config), sizeof(ghcm_stats),"
         " offsetof(ghcm_stats, device_ms), offsetof(ghcm_config, use_tma), sizeof(ghcm_instance),"
         " offsetof(ghcm_instance, input_is_speed), sizeof(ghcm_batch_info), offsetof(ghcm_batch_info, tma_instances),"
-        " sizeof(ghcm_tune_trial), offsetof(ghcm_tune_trial, ms)); return 0;}\n")
+        " sizeof(ghcm_tune_trial), offsetof(ghcm_tune_trial, ms), sizeof(ghcm_trace_record),"
+        " sizeof(ghcm_train_config), (size_t)GHCM_MLP_PARAMS); return 0;}\n")
     exe = tmp_path / "sizes"
     subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
                    check=True)
@@ -50,7 +51,8 @@ def test_struct_layouts_match_c(tmp_path):
                    _lib.GhcmStats.device_ms.offset, _lib.GhcmConfig.use_tma.offset,
                    ctypes.sizeof(_lib.GhcmInstance), _lib.GhcmInstance.input_is_speed.offset,
                    ctypes.sizeof(_lib.GhcmBatchInfo), _lib.GhcmBatchInfo.tma_instances.offset,
-                   ctypes.sizeof(_lib.GhcmTuneTrial), _lib.GhcmTuneTrial.ms.offset]
+                   ctypes.sizeof(_lib.GhcmTuneTrial), _lib.GhcmTuneTrial.ms.offset,
+                   ctypes.sizeof(_lib.GhcmTraceRecord), ctypes.sizeof(_lib.GhcmTrainConfig), _lib.GHCM_MLP_PARAMS]
 
 
 def test_header_compiles_as_cpp(tmp_path):
@@ -66,7 +68,7 @@ def test_defaults_mirror_the_reference_config(ghcm_lib):
     assert c.block_size == 16 and c.max_jobs == 0
     assert abs(c.eps - 1e-5) < 1e-12  # HcmConfig::fim_minimum_change (src/eikonal.h:24)
     assert c.kernel == _lib.GHCM_KERNEL_SYSTOLIC  # HcmConfig::kernel (src/eikonal.h:26)
-    assert c.use_tma == 1 and c.device == -1 and list(c.reserved) == [0] * 5
+    assert c.use_tma == 1 and c.device == -1 and c.fallback_jobs == 0 and list(c.reserved) == [0] * 4
 
 
 def test_status_strings(ghcm_lib):
@@ -141,3 +143,18 @@ def test_batch_calls_check_arguments(ghcm_lib):
     bad.block_size = 24
     assert ghcm_lib.ghcm_autotune_batch(ctypes.byref(bad), inst, 1, None, 1, ctypes.byref(best), None, 0,
                                         ctypes.byref(n)) == _lib.GHCM_ERR_BAD_ARG
+
+
+def test_learned_calls_check_arguments(ghcm_lib):
+    n = ctypes.c_uint32()
+    assert ghcm_lib.ghcm_trace_enable(None, 16) == _lib.GHCM_ERR_BAD_ARG
+    assert ghcm_lib.ghcm_trace_read(None, None, 0, ctypes.byref(n), None) == _lib.GHCM_ERR_BAD_ARG
+    assert ghcm_lib.ghcm_set_schedule_model(None, None, 0, 0.5) == _lib.GHCM_ERR_BAD_ARG
+    out = (ctypes.c_uint32 * 4)()
+    assert ghcm_lib.ghcm_schedule_counters(None, out) == _lib.GHCM_ERR_BAD_ARG
+    assert ghcm_lib.ghcm_mlp_forward(None, None, 4, None, None) == _lib.GHCM_ERR_BAD_ARG
+    assert ghcm_lib.ghcm_mlp_grad(None, None, None, 4, 1.0, None, None, None) == _lib.GHCM_ERR_BAD_ARG
+    tc = _lib.GhcmTrainConfig()
+    assert ghcm_lib.ghcm_train_config_default(ctypes.byref(tc)) == 0
+    assert tc.epochs > 0 and tc.batch > 0 and tc.lr > 0 and tc.pos_weight == 1.0 and list(tc.reserved) == [0] * 5
+    assert ghcm_lib.ghcm_mlp_train(None, None, 0, None, ctypes.byref(tc), None, None) == _lib.GHCM_ERR_BAD_ARG
