@@ -1,24 +1,32 @@
 """Benchmark of the gHCM block eikonal solve on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ghcm|reference]
+                    [--workload ring|batched]
 
-Workload (one "step" = one solve to convergence): the 4096 x 4096 seven-ring
-speed field (radii 256..1920, barrier width 16, speed 0.01, 64-cell gaps at
-seeded angles, one centre source, h = 1), tiles of 16 x 16, device top-n
-selection with n = 256 (the fastest of the configuration's n in {256, 1024,
-4096}; the other two are timed and reported beside it), eps = 1e-5. Synthetic, seeded input: the reference's
-ring images are replaced by the same construction drawn procedurally.
+Default workload (one "step" = one solve to convergence): the 4096 x 4096
+seven-ring speed field (radii 256..1920, barrier width 16, speed 0.01, 64-cell
+gaps at seeded angles, one centre source, h = 1), tiles of 16 x 16, the plain
+device top-n schedule with n = 256 (the configuration's other n, 1024 and
+4096, are timed and reported beside it), eps = 1e-5. Synthetic, seeded input:
+the reference's ring images are replaced by the same construction drawn
+procedurally. Beside it the line reports the error of the field against an
+FP64 FMM, and the learned schedule against the plain one on the 4096 x 4096
+fractal-noise field with 16 sources (model file from
+ghcm_gb300/train_schedule.py, trained on 32 other seeds).
 
-Metric: Mcell/s to convergence = W*H / (time from device-resident speed and
+--workload batched: 512 independent instances (side log-uniform in
+[64, 1024], multiples of 16, seven-ring or noise, 1-8 sources) in one
+persistent launch replayed from a CUDA graph, tile size / n / sweep cap from
+the autotuner; with N ranks the instances are split by cells (weak scaling).
+
+Metric: Mcell/s to convergence = cells / (time from device-resident speed and
 seeds to the device-resident converged time field). `value` is that, summed
-over all ranks; `e2e` is the same metric through the public host-pointer call
-(ghcm_solve: pinned host speed in, host time field out, copies inside the
-timed region). Multi-GPU runs are independent replicas (the single-grid solve
-does not shard), so scaling is weak.
+over all ranks; `e2e` is the same metric through the public calls with the
+host<->device copies of inputs and results inside the timed region.
 
 --impl reference times the reference's CPU solver (the FMM of
 src/eikonal_fmm.cpp as restated in oracle/, bit-exact to the reference build)
-on the same workload, one solve per host thread.
+on the same workload, over the host's cores.
 """
 from __future__ import annotations
 
@@ -37,9 +45,16 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "Mcell/s to convergence (plain device top-n schedule), 1 GB300, max rel err <=1e-5 vs reference FIM"
+
+METRIC = "Mcell/s to convergence, learned vs plain schedule, 1 GB300, max rel err \u22641e-5"
 UNIT = "Mcell/s"
 WORKLOAD = "ring7_4096x4096"
+BATCH_WORKLOAD = "batched_512_ring7_or_noise_64_to_1024"
+BATCH_COUNT = 512
+BATCH_SEED = 1234
+NOISE_EVAL_SEED = 1
+MODEL = ROOT / "ghcm_gb300" / "models" / "schedule_noise4096_b16.npz"
+LAUNCHES_PER_SOLVE = 3  # k_init_inst, k_init_seeds, the persistent k_solve
 BLOCK = 16
 N_JOBS = 256
 N_SWEEP = (256, 1024, 4096)
@@ -155,6 +170,26 @@ def load_traffic():
     return None
 
 
+def batch_instances():
+    from ghcm_gb300 import fields
+
+    return fields.batched_mix(BATCH_COUNT, seed=BATCH_SEED)
+
+
+def cpu_fmm_pool(o, insts, threads: int) -> float:
+    """Solves every instance once with the reference FMM over `threads` host
+    threads; returns wall microseconds."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from ghcm_gb300 import fields
+
+    costs = [(fields.cost_from_speed(i.speed), i.seeds) for i in insts]
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda cs: o.fmm(cs[0], cs[1]), costs))
+    return (time.perf_counter() - t0) * 1e6
+
+
 def run_reference(args, world, rank) -> int:
     if rank != 0:
         return 0
@@ -163,6 +198,27 @@ def run_reference(args, world, rank) -> int:
 
     build(with_reference=False)
     o = Oracle()
+    if args.workload == "batched":
+        insts = batch_instances()[::8]  # a fixed 1-in-8 sample of the batch per step
+        cells = sum(i.speed.size for i in insts)
+        threads = max(1, os.cpu_count() or 1)
+        for _ in range(args.warmup):
+            cpu_fmm_pool(o, insts[: threads], threads)
+        us = sum(cpu_fmm_pool(o, insts, threads) for _ in range(args.steps))
+        value = cells * args.steps / us
+        line = {
+            "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": us / 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": BATCH_WORKLOAD, "solver": "reference FMM (src/eikonal_fmm.cpp), CPU",
+                       "threads": threads},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"every 8th instance of the batch ({len(insts)} instances, {cells} cells) "
+                                       "per step, one instance per host thread at a time"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return 0
     speed, seeds = make_workload()
     cost = fields.cost_from_speed(speed)
     threads = max(1, min(os.cpu_count() or 1, args.steps))
@@ -184,6 +240,216 @@ def run_reference(args, world, rank) -> int:
     return 0
 
 
+def fmm64_errors(field: np.ndarray, ref64: np.ndarray) -> dict:
+    """L-inf and L1 (mean) absolute error of `field` against the FP64 FMM over
+    cells finite in both, with the largest relative error."""
+    f = field.astype(np.float64)
+    m = np.isfinite(f) & np.isfinite(ref64)
+    d = np.abs(f[m] - ref64[m])
+    pos = m & (ref64 > 0)
+    rel = np.abs(f[pos] - ref64[pos]) / ref64[pos]
+    return {"linf": float(d.max()) if d.size else 0.0, "l1": float(d.mean()) if d.size else 0.0,
+            "max_rel": float(rel.max()) if rel.size else 0.0,
+            "reachability_matches": bool(np.array_equal(np.isfinite(f), np.isfinite(ref64)))}
+
+
+def timed_device_solves(g, setup, d_speed, d_seeds, d_time, stream, flush, steps: int, warmup: int):
+    """`steps` device-resident solves timed with CUDA events on `stream`, the
+    L2 flushed before each (outside the events). Returns (mean ms, stats)."""
+    import torch
+
+    for _ in range(warmup):
+        g.solve_device(setup, d_speed, d_seeds, d_time, stream=stream)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    sts = []
+    for i in range(steps):
+        flush.fill_(float(i))
+        evs[i][0].record(stream)
+        sts.append(g.solve_device(setup, d_speed, d_seeds, d_time, stream=stream))
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) / steps, sts
+
+
+def learned_vs_plain(g, dev, stream, flush, steps: int, warmup: int) -> dict:
+    """The learned schedule against the plain one on the 4096^2 noise field
+    (16 sources, seed NOISE_EVAL_SEED, not among the model's training seeds)."""
+    import torch
+
+    from ghcm_gb300 import fields, learned
+    from oracle.oracle import rel_diff
+
+    if not MODEL.exists():
+        return {"unavailable": f"no model file {MODEL.name}: python -m ghcm_gb300.train_schedule writes it"}
+    params, threshold, meta = learned.load_model(MODEL)
+    speed, seeds = fields.value_noise(4096, seed=NOISE_EVAL_SEED, base_period=512.0, sources=16)
+    cells = speed.size
+    d_speed = torch.from_numpy(speed).to(dev)
+    d_seeds = torch.from_numpy(seeds.astype(np.int32)).to(dev)
+    runs = {
+        "plain_n1024": (g.HcmConfig(block_size=16, max_jobs=1024, fim_minimum_change=EPS), None),
+        "plain_n4096": (g.HcmConfig(block_size=16, max_jobs=4096, fim_minimum_change=EPS), None),
+        "learned_score_fb1024": (g.HcmConfig(block_size=16, max_jobs=4096, fallback_jobs=1024,
+                                             fim_minimum_change=EPS, schedule=g.Schedule.Learned), learned.POLICY_SCORE),
+        "learned_veto_n1024": (g.HcmConfig(block_size=16, max_jobs=1024, fim_minimum_change=EPS,
+                                           schedule=g.Schedule.Learned), learned.POLICY_VETO),
+    }
+    out, fields_out = {}, {}
+    for name, (cfg, policy) in runs.items():
+        d_time = torch.empty_like(d_speed)
+        with g.HcmSetup(cfg) as s:
+            if policy is not None:
+                learned.set_model(s, params, threshold)
+                learned.set_policy(s, policy)
+            ms, sts = timed_device_solves(g, s, d_speed, d_seeds, d_time, stream, flush, steps, warmup)
+            c = learned.counters(s) if policy is not None else {}
+        fields_out[name] = d_time.cpu().numpy()
+        out[name] = {"mcells": cells / (ms * 1e3), "ms": ms,
+                     "block_solves": statistics.mean(x["block_solves"] for x in sts),
+                     "waves": statistics.mean(x["waves"] for x in sts), **c}
+    base = out["plain_n1024"]["block_solves"]
+    for name in runs:
+        out[name]["solves_vs_plain_n1024"] = out[name]["block_solves"] / base
+        out[name]["max_rel_vs_plain_n1024"] = rel_diff(fields_out[name], fields_out["plain_n1024"])
+    return {"workload": "noise_4096x4096_16src", "seed": NOISE_EVAL_SEED, "threshold": threshold,
+            "model": MODEL.name, "train_seeds": int(len(meta.get("train_seeds", []))), "runs": out}
+
+
+def run_batched(args, world, rank, local) -> int:
+    """C4: the batch of independent instances in one persistent launch from a
+    CUDA graph, configured by the autotuner; ranks split the instances."""
+    import torch
+
+    import ghcm_gb300 as g
+    from ghcm_gb300 import fields
+    from oracle.oracle import Oracle, build, rel_diff
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    all_insts = batch_instances()
+    mine = g.shard_instances([i.speed.size for i in all_insts], world)[rank]
+    insts = [all_insts[i] for i in mine]
+    cells = sum(i.speed.size for i in insts)
+    total_cells = sum(i.speed.size for i in all_insts)
+    h_speed = [torch.from_numpy(i.speed).pin_memory() for i in insts]
+    h_time = [torch.empty(i.speed.shape, dtype=torch.float32).pin_memory() for i in insts]
+    dinst = [g.DeviceInstance(hs.to(dev), torch.from_numpy(i.seeds.astype(np.int32)).to(dev),
+                              torch.empty(i.speed.shape, dtype=torch.float32, device=dev))
+             for hs, i in zip(h_speed, insts)]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    t0 = time.perf_counter()
+    best, trials = g.autotune_batch(g.HcmConfig(block_size=16, fim_minimum_change=EPS), dinst, reps=1)
+    tune_s = time.perf_counter() - t0
+    setup = g.HcmSetup(best)
+    batch = g.Batch(setup, dinst)
+    info = batch.info()
+    for _ in range(args.warmup):
+        batch.run(stream)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = []
+    with Clocks(local) as clk:
+        barrier()
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            stats.append(batch.run(stream))
+            ev[i][1].record(stream)
+        barrier()
+    clocks = clk.summary()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = total_cells / (ms * 1e3)
+
+    # end to end: pinned host fields in, every time field out, inside the timed region
+    e2e = []
+    for _ in range(max(1, min(args.steps, 3))):
+        barrier()
+        t0 = time.perf_counter()
+        for hs, di in zip(h_speed, dinst):
+            di.d_field.copy_(hs, non_blocking=True)
+        batch.run(stream)
+        for ht, di in zip(h_time, dinst):
+            ht.copy_(di.d_time, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = sum(e2e) / len(e2e)
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    B = info["block_size"]
+    solves = statistics.mean(st["block_solves"] for st in stats)
+    achieved = solves * bytes_per_solve(B) / (ms * 1e-3) / 1e9
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": BATCH_WORKLOAD, "instances": len(all_insts), "cells": total_cells,
+                   "instances_this_rank": len(insts), "block": B, "n": info["max_jobs"],
+                   "max_sweeps": info["max_sweeps"], "cuda_graph": bool(info["graph"]), "eps": EPS,
+                   "tma_instances": info["tma_instances"], "autotune_s": tune_s,
+                   "l2": "flushed between steps (256 MiB write outside the events)",
+                   "parallelism": f"instances split over {world} rank(s)"},
+        "e2e": {"value": total_cells / (e2e_ms * 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": sum(4 * i.speed.size for i in insts),
+                "d2h_bytes_per_step": sum(4 * i.speed.size for i in insts)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": f"k_solve<{B},systolic> (batch)",
+                     "bytes_per_block_solve": bytes_per_solve(B), "block_solves": solves,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in peaks else "fallback"},
+        "autotune": trials,
+        "gpu_launches": LAUNCHES_PER_SOLVE * args.steps,
+        "clocks": clocks,
+        "solver": {"waves": statistics.mean(st["waves"] for st in stats),
+                   "residual_passes": statistics.mean(st["residual_passes"] for st in stats),
+                   "max_active": max(st["max_active"] for st in stats)},
+    }
+    if rank == 0:
+        build(with_reference=False)
+        o = Oracle()
+        # parity on a fixed sample of this rank's instances against the reference FIM
+        worst = 0.0
+        for k in range(0, len(insts), max(1, len(insts) // 8)):
+            inst = insts[k]
+            ref = o.fim(fields.cost_from_speed(inst.speed), inst.seeds, EPS)[0]
+            worst = max(worst, rel_diff(dinst[k].d_time.cpu().numpy(), ref))
+        line["check"] = {"max_rel_vs_fim_sample": worst, "sample": "every len/8-th instance of rank 0"}
+        if not args.no_cpu_baseline:
+            sample = all_insts[::8]
+            threads = max(1, os.cpu_count() or 1)
+            us = cpu_fmm_pool(o, sample, threads)
+            sc = sum(i.speed.size for i in sample)
+            line["cpu_baseline"] = {"value": sc / us, "unit": UNIT, "cores": threads, "kind": "port",
+                                    "sample": f"every 8th instance ({len(sample)} instances, {sc} cells), reference "
+                                              "FMM, one instance per host thread at a time",
+                                    "cpu": _cpu_name()}
+        print(json.dumps(line), flush=True)
+    batch.close()
+    setup.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -195,10 +461,14 @@ def main() -> int:
     ap.add_argument("--kernel", default="systolic", choices=["systolic", "fim"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-n-sweep", action="store_true", help="time only the headline n")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain comparison")
+    ap.add_argument("--workload", default="ring", choices=["ring", "batched"])
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, world, rank)
+    if args.workload == "batched":
+        return run_batched(args, world, rank, local)
 
     import torch
 
@@ -320,7 +590,7 @@ def main() -> int:
                      "bytes_per_block_solve": bps, "block_solves": solves, "kernel_ms": k_ms,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in peaks else "fallback"},
         "n_sweep": n_sweep,
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": LAUNCHES_PER_SOLVE * args.steps,
         "clocks": clocks,
         "solver": {"waves": statistics.mean(st["waves"] for st in stats),
                    "residual_passes": statistics.mean(st["residual_passes"] for st in stats),
@@ -341,6 +611,11 @@ def main() -> int:
             line["check"]["max_rel_vs_fim"] = rel_diff(field, fim)
             line["check"]["max_rel_vs_fmm"] = rel_diff(field, fmm)
             line["check"]["fim_vs_fmm"] = rel_diff(fim, fmm)
+            ref64, _ = Oracle().fmm64(cost, seeds)
+            line["check"]["vs_fmm64"] = fmm64_errors(field, ref64)
+            line["check"]["fim_vs_fmm64"] = fmm64_errors(fim, ref64)
+        if not args.no_learned:
+            line["learned_vs_plain"] = learned_vs_plain(g, dev, stream, flush, max(1, min(args.steps, 3)), 1)
         print(json.dumps(line), flush=True)
     setup.close()
     if dist is not None:
