@@ -50,6 +50,9 @@ METRIC = "Mcell/s to convergence, learned vs plain schedule, 1 GB300, max rel er
 UNIT = "Mcell/s"
 WORKLOAD = "ring7_4096x4096"
 BATCH_WORKLOAD = "batched_512_ring7_or_noise_64_to_1024"
+MAZE_WORKLOAD = "ca_maze_16384x16384_64src"
+MAZE_SEED = 5
+MAZE_CROP = 2048
 BATCH_COUNT = 512
 BATCH_SEED = 1234
 NOISE_EVAL_SEED = 1
@@ -450,6 +453,100 @@ def run_batched(args, world, rank, local) -> int:
     return 0
 
 
+def run_maze(args, world, rank, local) -> int:
+    """C5: the 16384^2 cellular-automaton maze (wall speed 0.001, open 1.0, 64
+    sources in open cells, ~2 GB of device state): a short tile-size / n sweep,
+    the best timed, and the error against an FP64 FMM of the whole field
+    reported on the central 2048^2 crop."""
+    import torch
+
+    import ghcm_gb300 as g
+    from ghcm_gb300 import fields
+    from oracle.oracle import Oracle, build
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    t0 = time.perf_counter()
+    speed, seeds = fields.ca_maze(16384, seed=MAZE_SEED)
+    gen_s = time.perf_counter() - t0
+    cells = speed.size
+    d_speed = torch.from_numpy(speed).to(dev)
+    d_seeds = torch.from_numpy(seeds.astype(np.int32)).to(dev)
+    d_time = torch.empty_like(d_speed)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    sweep = {}
+    best = None
+    for block, n in ((16, 4096), (16, 16384), (32, 4096), (32, 16384)):
+        cfg = g.HcmConfig(block_size=block, max_jobs=n, fim_minimum_change=EPS)
+        with g.HcmSetup(cfg) as s:
+            ms, sts = timed_device_solves(g, s, d_speed, d_seeds, d_time, stream, flush, 1, 1)
+        sweep[f"b{block}_n{n}"] = {"ms": ms, "mcells": cells / (ms * 1e3), "block_solves": sts[0]["block_solves"],
+                                   "waves": sts[0]["waves"]}
+        if best is None or ms < best[2]:
+            best = (block, n, ms)
+    block, n, _ = best
+    setup = g.HcmSetup(g.HcmConfig(block_size=block, max_jobs=n, fim_minimum_change=EPS))
+    with Clocks(local) as clk:
+        ms, stats = timed_device_solves(g, setup, d_speed, d_seeds, d_time, stream, flush, args.steps, args.warmup)
+    clocks = clk.summary()
+    value = cells / (ms * 1e3)
+    h_speed = torch.from_numpy(speed).pin_memory()
+    h_time = torch.empty_like(h_speed).pin_memory()
+    e2e = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        g.eikonal_hcm_cuda_ex(setup, h_speed.numpy(), seeds, input_is_speed=True, out=h_time.numpy())
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = min(e2e)
+    g.solve_device(setup, d_speed, d_seeds, d_time, stream=stream)
+    field = d_time.cpu().numpy()
+    solves = statistics.mean(st["block_solves"] for st in stats)
+    k_ms = statistics.mean(st["kernel_ms"] for st in stats)
+    achieved = solves * bytes_per_solve(block) / (k_ms * 1e-3) / 1e9
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": MAZE_WORKLOAD, "seed": MAZE_SEED, "block": block, "n": n, "eps": EPS,
+                   "sources": int(len(seeds)), "generate_s": gen_s,
+                   "device_state_gb": 2 * 4 * cells / 1e9, "l2": "flushed between steps"},
+        "e2e": {"value": cells / (e2e_ms * 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": 4 * cells + int(seeds.nbytes), "d2h_bytes_per_step": 4 * cells},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": f"k_solve<{block},systolic>", "bytes_per_block_solve":
+                         bytes_per_solve(block), "block_solves": solves, "kernel_ms": k_ms},
+        "sweep": sweep,
+        "gpu_launches": LAUNCHES_PER_SOLVE * args.steps,
+        "clocks": clocks,
+        "solver": {"waves": statistics.mean(st["waves"] for st in stats),
+                   "residual_passes": statistics.mean(st["residual_passes"] for st in stats),
+                   "max_active": max(st["max_active"] for st in stats)},
+    }
+    if rank == 0:
+        build(with_reference=False)
+        o = Oracle()
+        cost = fields.cost_from_speed(speed)
+        line["check"] = {"residual": o.residual(cost, field), "finite": bool(np.isfinite(field).all()),
+                         "seeds_zero": bool(np.all(field[seeds[:, 1], seeds[:, 0]] == 0))}
+        if not args.no_cpu_baseline:
+            t0 = time.perf_counter()
+            ref64, us64 = o.fmm64(cost, seeds)
+            c0 = (16384 - MAZE_CROP) // 2
+            crop = (slice(c0, c0 + MAZE_CROP), slice(c0, c0 + MAZE_CROP))
+            line["check"]["vs_fmm64_crop"] = {**fmm64_errors(field[crop], ref64[crop]),
+                                              "crop": f"[{c0}:{c0 + MAZE_CROP}]^2"}
+            line["check"]["vs_fmm64_full"] = fmm64_errors(field, ref64)
+            line["cpu_baseline"] = {"value": cells / us64, "unit": UNIT, "cores": 1, "kind": "port",
+                                    "sample": "one FP64 FMM of the whole field (the accuracy oracle), 1 host thread",
+                                    "cpu": _cpu_name()}
+        print(json.dumps(line), flush=True)
+    setup.close()
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -462,13 +559,15 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-n-sweep", action="store_true", help="time only the headline n")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain comparison")
-    ap.add_argument("--workload", default="ring", choices=["ring", "batched"])
+    ap.add_argument("--workload", default="ring", choices=["ring", "batched", "maze"])
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, world, rank)
     if args.workload == "batched":
         return run_batched(args, world, rank, local)
+    if args.workload == "maze":
+        return run_maze(args, world, rank, local)
 
     import torch
 
