@@ -75,7 +75,8 @@ class GhcmConfig(ctypes.Structure):
         ("device", ctypes.c_int32),
         ("use_tma", ctypes.c_uint32),
         ("fallback_jobs", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32 * 4),
+        ("cost_cap", ctypes.c_float),
+        ("reserved", ctypes.c_uint32 * 3),
     ]
 
 

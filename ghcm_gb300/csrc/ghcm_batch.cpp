@@ -134,6 +134,7 @@ int ghcm_batch_create(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count,
         I.in_is_speed = insts[i].input_is_speed ? 1u : 0u;
         I.seeds = insts[i].seeds_xy;
         I.n_seeds = insts[i].n_seeds;
+        I.cost_cap = cost_cap_of(ctx->cfg);
         tiles += static_cast<uint64_t>(I.tiles_x) * I.tiles_y;
         uint64_t const c = static_cast<uint64_t>(I.w) * I.h;
         cells += c;

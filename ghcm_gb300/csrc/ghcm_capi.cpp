@@ -26,6 +26,7 @@ int check_config(const ghcm_config* c) {
     if (c->kernel > GHCM_KERNEL_FIM || c->schedule > GHCM_SCHEDULE_LEARNED || c->key_mode > GHCM_KEY_BLOCK_MIN)
         return GHCM_ERR_BAD_ARG;
     if (!(c->eps >= 0.f) || !std::isfinite(c->eps)) return GHCM_ERR_BAD_ARG;
+    if (!(c->cost_cap >= 0.f)) return GHCM_ERR_BAD_ARG;  // NaN or negative
     for (uint32_t r : c->reserved)
         if (r != 0) return GHCM_ERR_BAD_ARG;
     return GHCM_OK;
@@ -116,6 +117,7 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     I.in_is_speed = input_is_speed ? 1u : 0u;
     I.seeds = d_seeds;
     I.n_seeds = n_seeds;
+    I.cost_cap = cost_cap_of(ctx->cfg);
     bool const aligned = (w % 4u == 0u) && (reinterpret_cast<uintptr_t>(d_field) % 16u == 0u) &&
                          (reinterpret_cast<uintptr_t>(d_time) % 16u == 0u);
     I.tma = 0;

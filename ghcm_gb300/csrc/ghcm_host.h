@@ -79,6 +79,11 @@ inline int status_from_error(uint32_t error) {
 // write (B^2).
 inline uint32_t bytes_per_solve(uint32_t b) { return 4u * b * b + 4u * ((b + 2u) * (b + 2u) - 4u) + 4u * b * b; }
 
+// The cost cap of a config (+inf when off).
+inline float cost_cap_of(const ghcm_config& cfg) {
+    return cfg.cost_cap > 0.f ? cfg.cost_cap : __builtin_huge_valf();
+}
+
 // Scheduler parameters of a config on a device with `sms` SMs.
 inline void fill_sched_params(Sched& s, const ghcm_config& cfg, int sms, uint32_t tiles) {
     uint32_t const B = cfg.block_size;

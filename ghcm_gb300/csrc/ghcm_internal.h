@@ -40,7 +40,7 @@ struct Inst {
     int32_t      tma;        // 1: tiles of this instance are staged by TMA (maps in Sched)
     const uint32_t* seeds;   // n_seeds (x, y) pairs on the device
     uint32_t     n_seeds;
-    uint32_t     pad0;
+    float        cost_cap;   // cost = min(cost, cost_cap); +inf = no cap
 };
 
 // Device-side control block of one solve.

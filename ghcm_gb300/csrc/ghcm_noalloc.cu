@@ -108,6 +108,7 @@ extern "C" int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_
     inst.in_is_speed = input_is_speed ? 1u : 0u;
     inst.seeds = d_seeds_xy;
     inst.n_seeds = n_seeds;
+    inst.cost_cap = cost_cap_of(*cfg);
     bool const aligned = (width % 4u == 0u) && (reinterpret_cast<uintptr_t>(d_field) % 16u == 0u) &&
                          (reinterpret_cast<uintptr_t>(d_time_out) % 16u == 0u);
     EncodeTiledFn const enc = tensor_map_encoder();

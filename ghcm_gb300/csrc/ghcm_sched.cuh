@@ -60,9 +60,12 @@ __device__ __forceinline__ int neighbour_tile(const Inst& I, uint32_t tx, uint32
     return static_cast<int>(I.tile_base) + ny * static_cast<int>(I.tiles_x) + nx;
 }
 
-// cost = h / speed (src/test_runner.cpp:38-42), IEEE-rounded like the host's.
+// cost = h / speed (src/test_runner.cpp:38-42), IEEE-rounded like the host's,
+// then capped: min(cost, cap) makes walls permeable as the reference's
+// field_cost_as_permeable does (src/test_runner.cpp:70-75); cap = +inf: none.
+__device__ __forceinline__ float cap_cost(const Inst& I, float c) { return fminf(c, I.cost_cap); }
 __device__ __forceinline__ float to_cost(const Inst& I, float v) {
-    return I.in_is_speed ? __fdiv_rn(I.spacing, v) : v;
+    return cap_cost(I, I.in_is_speed ? __fdiv_rn(I.spacing, v) : v);
 }
 
 // Puts `tile` into the next active set: lowers its key to `key`, ORs `bits`

@@ -137,7 +137,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
             sm.time[k] = f_inf();
             sm.cost[k] = f_inf();
         } else if (use_tma) {
-            if (I.in_is_speed) sm.cost[k] = __fdiv_rn(I.spacing, sm.cost[k]);
+            sm.cost[k] = to_cost(I, sm.cost[k]);
         } else {
             size_t const gi = static_cast<size_t>(gy) * I.w + gx;
             sm.time[k] = __ldcg(&I.time[gi]);

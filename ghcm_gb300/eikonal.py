@@ -68,6 +68,7 @@ class HcmConfig:
     use_tma: bool = True
     device: int = -1
     fallback_jobs: int = 0                 # learned schedule: n of a wave in which no tile qualifies
+    cost_cap: float = 0.0                  # > 0: cost = min(cost, cost_cap) (field_cost_as_permeable)
 
     def to_c(self, sm_count: int | None = None) -> GhcmConfig:
         c = GhcmConfig()
@@ -87,6 +88,7 @@ class HcmConfig:
         c.device = int(self.device)
         c.use_tma = 1 if self.use_tma else 0
         c.fallback_jobs = int(self.fallback_jobs)
+        c.cost_cap = float(self.cost_cap)
         return c
 
 

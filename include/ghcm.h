@@ -70,7 +70,10 @@ typedef struct ghcm_config {
     uint32_t use_tma;         /* 1 = stage tiles with TMA when the field allows it; 0 = plain loads */
     uint32_t fallback_jobs;   /* learned schedule: n of the plain top-n of a wave in which no tile
                                  qualifies; 0 = max_jobs */
-    uint32_t reserved[4];     /* must be zero */
+    float    cost_cap;        /* > 0: cost = min(cost, cost_cap), the reference's permeable-wall
+                                 transform field_cost_as_permeable (src/test_runner.cpp:70-75,
+                                 default there 1e3); 0 = no cap */
+    uint32_t reserved[3];     /* must be zero */
 } ghcm_config;
 
 typedef struct ghcm_stats {

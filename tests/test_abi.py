@@ -68,7 +68,7 @@ def test_defaults_mirror_the_reference_config(ghcm_lib):
     assert c.block_size == 16 and c.max_jobs == 0
     assert abs(c.eps - 1e-5) < 1e-12  # HcmConfig::fim_minimum_change (src/eikonal.h:24)
     assert c.kernel == _lib.GHCM_KERNEL_SYSTOLIC  # HcmConfig::kernel (src/eikonal.h:26)
-    assert c.use_tma == 1 and c.device == -1 and c.fallback_jobs == 0 and list(c.reserved) == [0] * 4
+    assert c.use_tma == 1 and c.device == -1 and c.fallback_jobs == 0 and c.cost_cap == 0.0 and list(c.reserved) == [0] * 3
 
 
 def test_status_strings(ghcm_lib):
@@ -158,3 +158,13 @@ def test_learned_calls_check_arguments(ghcm_lib):
     assert ghcm_lib.ghcm_train_config_default(ctypes.byref(tc)) == 0
     assert tc.epochs > 0 and tc.batch > 0 and tc.lr > 0 and tc.pos_weight == 1.0 and list(tc.reserved) == [0] * 5
     assert ghcm_lib.ghcm_mlp_train(None, None, 0, None, ctypes.byref(tc), None, None) == _lib.GHCM_ERR_BAD_ARG
+
+
+def test_cost_cap_must_be_a_non_negative_number(ghcm_lib):
+    c = _lib.GhcmConfig()
+    ghcm_lib.ghcm_config_default(ctypes.byref(c))
+    h = ctypes.c_void_p()
+    for bad in (-1.0, float("nan")):
+        x = _lib.GhcmConfig.from_buffer_copy(c)
+        x.cost_cap = bad
+        assert ghcm_lib.ghcm_create(ctypes.byref(x), ctypes.byref(h)) == _lib.GHCM_ERR_BAD_ARG

@@ -267,3 +267,22 @@ def test_abi_call_directly(ghcm_lib, cuda_ok):
         assert out[0, 5] == 5.0 and out[5, 0] == 5.0 and st.block_solves > 0
     finally:
         ghcm_lib.ghcm_destroy(h)
+
+
+@pytest.mark.parametrize("block", [8, 16, 32])
+def test_permeable_cost_cap(setups, oracle_lib, block):
+    """cost = min(cost, cap), the reference's field_cost_as_permeable
+    (src/test_runner.cpp:70-75): speed-0 walls become passable at cost 1e3."""
+    rng = np.random.default_rng(40 + block)
+    speed = rng.uniform(0.3, 1.0, size=(150, 170)).astype(np.float32)
+    speed[40:44, :150] = 0.0  # a wall with no gap on the left side
+    speed[100:130, 60:64] = 0.0
+    seeds = np.array([[20, 10], [160, 140]], dtype=np.uint32)
+    capped = np.minimum(fields.cost_from_speed(speed), np.float32(1e3))
+    ref = oracle_lib.fim(capped, seeds, 1e-5)[0]
+    assert np.isfinite(ref).all()
+    res = g.eikonal_hcm_cuda_ex(setups(block, cost_cap=1e3), speed, seeds, input_is_speed=True)
+    check_field(res.field, ref, seeds)
+    # the cost form of the input gives the same field
+    res2 = g.eikonal_hcm_cuda_ex(setups(block, cost_cap=1e3), fields.cost_from_speed(speed), seeds)
+    check_field(res2.field, ref, seeds)
