@@ -95,8 +95,13 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_
             uint32_t const wave = s_state[kStWaves];
             const uint32_t* jobs = s_state[kStInList] ? s.list[cur] : s.jobs;
             for (uint32_t j = blockIdx.x; j < nj; j += gridDim.x) {
-                int const r = solve_tile<B, FIM>(s, __ldcg(&jobs[j]), cur ^ 1u, sm, &s_bar, parity, tma_pending,
-                                                 s_word, s_red, s_krange, wave);
+                uint32_t const job = __ldcg(&jobs[j]);
+                if (job >= s.num_tiles) {  // never written by a correct decision: stop the grid
+                    if (tid == 0) atomicOr(&ctl->error, kErrInternal);
+                    break;
+                }
+                int const r = solve_tile<B, FIM>(s, job, cur ^ 1u, sm, &s_bar, parity, tma_pending, s_word, s_red,
+                                                 s_krange, wave);
                 if (r == kJobFailed) break;
                 solves += (r == kJobSolved) ? 1u : 0u;
             }
@@ -162,7 +167,12 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
             uint32_t const wave = s_state[kStWaves];
             const uint32_t* jobs = s_state[kStInList] ? s.list[cur] : s.jobs;
             for (uint32_t j = gw; j < nj; j += nwarps) {
-                int const r = solve_tile_warp<B>(s, __ldcg(&jobs[j]), cur ^ 1u, sm, parity, tma_pending, s_krange, wave);
+                uint32_t const job = __ldcg(&jobs[j]);
+                if (job >= s.num_tiles) {
+                    if (lane == 0) atomicOr(&ctl->error, kErrInternal);
+                    break;
+                }
+                int const r = solve_tile_warp<B>(s, job, cur ^ 1u, sm, parity, tma_pending, s_krange, wave);
                 if (r == kJobFailed) break;
                 solves += (r == kJobSolved) ? 1u : 0u;
             }
