@@ -116,7 +116,7 @@ __device__ __forceinline__ uint32_t tile_key(const Sched& s, uint32_t tile) {
 // order is exact up to 1/SELECT_BINS of the range. Returns the number carried.
 constexpr int SELECT_BINS = 2048;
 
-template <int THREADS>
+template <int THREADS, int CACHE>
 __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t m, uint32_t n, uint32_t* carry,
                                  uint32_t* s_hist, uint32_t* s_sel, float lo, float hi, bool have_range,
                                  uint32_t jobs_base) {
@@ -161,8 +161,28 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
         int const b = static_cast<int>((k - lo) * scale);
         return b < 0 ? 0 : (b >= SELECT_BINS ? SELECT_BINS - 1 : b);
     };
-    // pass 2: histogram (four keys in flight per thread)
-    {
+    // pass 2: histogram. Up to CACHE entries per thread (a register budget set
+    // by the kernel) keep their key in registers for the gather pass (lists of
+    // up to THREADS * CACHE tiles), so it re-reads only the coalesced list;
+    // longer lists load keys again there.
+    bool const cached = m <= static_cast<uint32_t>(THREADS * CACHE);
+    uint32_t ck[CACHE];
+    if (cached) {
+        uint32_t ct[CACHE];
+#pragma unroll
+        for (int u = 0; u < CACHE; ++u) {
+            uint32_t const i = tid + u * THREADS;
+            ct[u] = (i < m) ? __ldcg(&list[i]) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < CACHE; ++u) {
+            uint32_t const i = tid + u * THREADS;
+            ck[u] = (i < m) ? tile_key(s, ct[u]) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < CACHE; ++u)
+            if (tid + u * THREADS < m) atomicAdd(&s_hist[bin_of(__uint_as_float(ck[u]))], 1u);
+    } else {
         uint32_t i = tid;
         for (; i + 3u * THREADS < m; i += 4u * THREADS) {
             uint32_t t4[4];
@@ -215,15 +235,26 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
     int const bnd = static_cast<int>(s_sel[0]);
     uint32_t const take_eq = s_sel[1];
     // pass 3: gather
-    for (uint32_t i = tid; i < m; i += THREADS) {
-        uint32_t const t = __ldcg(&list[i]);
-        int const b = bin_of(__uint_as_float(tile_key(s, t)));
+    auto place = [&](uint32_t t, uint32_t kb) {
+        int const b = bin_of(__uint_as_float(kb));
         bool take = b < bnd;
         if (!take && b == bnd) take = atomicAdd(&s_sel[2], 1u) < take_eq;
         if (take)
             s.jobs[jobs_base + atomicAdd(&s_sel[3], 1u)] = t;
         else
             carry[atomicAdd(&s_sel[4], 1u)] = t;
+    };
+    if (cached) {
+#pragma unroll
+        for (int u = 0; u < CACHE; ++u) {
+            uint32_t const i = tid + u * THREADS;
+            if (i < m) place(__ldcg(&list[i]), ck[u]);
+        }
+    } else {
+        for (uint32_t i = tid; i < m; i += THREADS) {
+            uint32_t const t = __ldcg(&list[i]);
+            place(t, tile_key(s, t));
+        }
     }
     __syncthreads();
     return s_sel[4];
@@ -271,14 +302,14 @@ __device__ __forceinline__ float ld_relaxed_f(const float* p) { return __uint_as
 // base.. of the next JOBS phase (or, with no jobs before them and m <= n, the
 // list itself), the rest is carried to list[L ^ 1], where the activations of
 // that phase also go. Returns {in_list, job count} in s_sel[8], [11].
-template <int THREADS>
+template <int THREADS, int CACHE>
 __device__ void plan_plain_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t n, uint32_t base, float lo, float hi,
                                 uint32_t* s_hist, uint32_t* s_sel) {
     Ctl* ctl = s.ctl;
     bool const all = m <= n;
     uint32_t carried = 0u;
     if (!all) {
-        carried = select_top_n<THREADS>(s, s.list[L], m, n, s.list[L ^ 1u], s_hist, s_sel, lo, hi, s.key_mode == 0u,
+        carried = select_top_n<THREADS, CACHE>(s, s.list[L], m, n, s.list[L ^ 1u], s_hist, s_sel, lo, hi, s.key_mode == 0u,
                                         base);
     } else if (base) {
         for (uint32_t i = threadIdx.x; i < m; i += THREADS) s.jobs[base + i] = __ldcg(&s.list[L][i]);
@@ -306,7 +337,7 @@ __device__ void plan_plain_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t
 //   the carried set in plain key order (all of the wave when it took none).
 // The key range of list[act] comes from the activations (ctl->krange); its
 // min and span are published as this wave's front for the features.
-template <int THREADS>
+template <int THREADS, int CACHE>
 __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_hist, uint32_t* s_sel) {
     Ctl* ctl = s.ctl;
     int const tid = threadIdx.x;
@@ -330,7 +361,7 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
         } else {
             float const lo = __uint_as_float(ld_relaxed(&ctl->krange[L][0]));
             float const hi = __uint_as_float(ld_relaxed(&ctl->krange[L][1]));
-            plan_plain_jobs<THREADS>(s, L, m, want - take, take, lo, hi, s_hist, s_sel);
+            plan_plain_jobs<THREADS, CACHE>(s, L, m, want - take, take, lo, hi, s_hist, s_sel);
             ncur = L;
             if (tid == 0) atomicAdd(take ? &ctl->score_waves : &ctl->fallback_waves, 1u);
         }
@@ -382,7 +413,7 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
                     s_sel[11] = m;  // tiles to score
                 }
             } else {
-                plan_plain_jobs<THREADS>(s, act, m, s.max_jobs, 0u, lo, hi, s_hist, s_sel);
+                plan_plain_jobs<THREADS, CACHE>(s, act, m, s.max_jobs, 0u, lo, hi, s_hist, s_sel);
                 if (tid == 0) atomicAdd(&ctl->waves, 1u);
             }
         }
@@ -398,7 +429,7 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
 // that carries the decision, so a released CTA needs no further load. The
 // waits are bounded. On return s_state holds the new state; returns false
 // when the grid must stop (timeout or error).
-template <int THREADS>
+template <int THREADS, int CACHE>
 __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, uint32_t* s_state,
                              uint32_t* s_krange) {
     __shared__ uint32_t s_last;
@@ -432,7 +463,7 @@ __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, 
             ctl->wave_max_sweeps = 0u;
         }
 #endif
-        decide_phase<THREADS>(s, s_state, s_hist, s_sel);
+        decide_phase<THREADS, CACHE>(s, s_state, s_hist, s_sel);
         __syncthreads();
         if (threadIdx.x == 0) {
             uint32_t const err = ld_relaxed(&ctl->error);

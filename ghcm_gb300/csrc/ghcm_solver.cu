@@ -51,6 +51,13 @@ constexpr int max_ctas_per_sm() {
     return B == 8 ? 12 : 4;
 }
 
+// Keys per thread the top-n select keeps in registers between its passes: as
+// many as fit in the kernel's register budget without spills.
+template <int B, bool FIM>
+__host__ __device__ constexpr int select_cache() {
+    return B == 32 ? (FIM ? 1 : 2) : 4;
+}
+
 template <int B, bool FIM>
 __global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_solve(const __grid_constant__ Sched s) {
     using G = TileGeom<B>;
@@ -84,7 +91,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_
     uint32_t const nwarps = gridDim.x * warps_per_cta;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
-        bool const ok = wave_barrier<G::THREADS>(s, s_hist, s_sel, s_state, s_krange);
+        bool const ok = wave_barrier<G::THREADS, select_cache<B, FIM>()>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
         uint32_t const phase = s_state[kStPhase];
@@ -156,7 +163,7 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
     uint32_t const nwarps = gridDim.x * W::NW;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
-        bool const ok = wave_barrier<W::THREADS>(s, s_hist, s_sel, s_state, s_krange);
+        bool const ok = wave_barrier<W::THREADS, 4>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
         uint32_t const phase = s_state[kStPhase];
