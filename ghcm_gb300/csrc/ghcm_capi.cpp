@@ -184,6 +184,11 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
                  c.prof[2] / 1e3 / std::max(1ull, c.prof[9]), c.prof[6] / 1e3 / std::max(1ull, c.prof[9]),
                  c.prof[7] / 1e3 / std::max(1ull, c.prof[9]) / std::max(1, grid - 1),
                  double(c.prof[8]) / std::max(1ull, c.prof[9]), double(c.prof[3]) / std::max(1ull, c.block_solves));
+    if (c.prof[13])
+        std::fprintf(stderr, "[ghcm-prof] per CTA block-solve: stage %.2f us, sweeps %.2f us (%.3f us/sweep), "
+                     "probe+commit+activate %.2f us\n",
+                     c.prof[10] / 1e3 / c.prof[13], c.prof[11] / 1e3 / c.prof[13],
+                     c.prof[11] / 1e3 / std::max(1ull, c.prof[3]), c.prof[12] / 1e3 / c.prof[13]);
 #endif
     if (stats) {
         float ms = 0.f, kms = 0.f;

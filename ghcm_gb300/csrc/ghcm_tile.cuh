@@ -79,6 +79,9 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     TileCoord const tc = tile_coord<B>(I, tile);
     bool const use_tma = I.tma != 0;
 
+#ifdef GHCM_PROFILE
+    uint64_t const p_t0 = (tid == 0) ? global_ns() : 0ull;
+#endif
     // Claim: clear the tile's activation state (a later activation re-queues
     // it), then stage the tile with its halo.
     if (tid == 0) {
@@ -146,6 +149,9 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     }
     __syncthreads();
     if (s_word[1]) return kJobFailed;
+#ifdef GHCM_PROFILE
+    uint64_t const p_t1 = (tid == 0) ? global_ns() : 0ull;
+#endif
 
     constexpr int BW = G::BW;
     float t[G::CPT], t0[G::CPT], c[G::CPT], c2[G::CPT];
@@ -267,6 +273,9 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         }
     }
 
+#ifdef GHCM_PROFILE
+    uint64_t const p_t2 = (tid == 0) ? global_ns() : 0ull;
+#endif
     // Which edge rows this solve changed (bit e: the row facing neighbour e).
     {
         uint32_t ec = 0u;
@@ -357,6 +366,11 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     }
 #ifdef GHCM_PROFILE
     if (tid == 0) {
+        uint64_t const p_t3 = global_ns();
+        atomicAdd(&s.ctl->prof[10], static_cast<unsigned long long>(p_t1 - p_t0));
+        atomicAdd(&s.ctl->prof[11], static_cast<unsigned long long>(p_t2 - p_t1));
+        atomicAdd(&s.ctl->prof[12], static_cast<unsigned long long>(p_t3 - p_t2));
+        atomicAdd(&s.ctl->prof[13], 1ull);
         atomicAdd(&s.ctl->prof[3], static_cast<unsigned long long>(sweeps));
         atomicMax(&s.ctl->wave_max_sweeps, sweeps);
     }
