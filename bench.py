@@ -493,6 +493,7 @@ def run_maze(args, world, rank, local) -> int:
     value = cells / (ms * 1e3)
     h_speed = torch.from_numpy(speed).pin_memory()
     h_time = torch.empty_like(h_speed).pin_memory()
+    g.eikonal_hcm_cuda_ex(setup, h_speed.numpy(), seeds, input_is_speed=True, out=h_time.numpy())  # warm-up
     e2e = []
     for _ in range(2):
         t0 = time.perf_counter()
@@ -657,6 +658,8 @@ def main() -> int:
     # end to end through the host-pointer call: pinned speed in, time field out
     h_speed = torch.from_numpy(speed).pin_memory()
     h_time = torch.empty((h, w), dtype=torch.float32).pin_memory()
+    # untimed warm-up: the first host-pointer call sizes the context's staging buffers
+    g.eikonal_hcm_cuda_ex(setup, h_speed.numpy(), seeds, input_is_speed=True, out=h_time.numpy())
     e2e_ms = []
     for i in range(max(1, min(args.steps, 5))):
         t0 = time.perf_counter()
