@@ -33,7 +33,7 @@ namespace ghcm {
 namespace {
 
 constexpr size_t kSlot = static_cast<size_t>(GHCM_NOALLOC_MAX_TILES) * sizeof(uint32_t);
-constexpr size_t kCtlBytes = 256;
+constexpr size_t kCtlBytes = 512;
 constexpr size_t kInstBytes = 256;
 // flags | key | tmin | list0 | list1 | jobs | control block | instance
 constexpr size_t kScratchBytes = 6 * kSlot + kCtlBytes + kInstBytes;

@@ -461,6 +461,10 @@ __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, 
             if (ctl->release_ns) ctl->prof[6] += t_last - ctl->release_ns;  // release -> last arrival
             ctl->prof[8] += ctl->wave_max_sweeps;
             ctl->wave_max_sweeps = 0u;
+            ctl->prof[15] += ctl->prof[14];  // per-wave maxima: job end, first-job start, longest solve
+            ctl->prof[17] += ctl->prof[16];
+            ctl->prof[19] += ctl->prof[18];
+            ctl->prof[14] = ctl->prof[16] = ctl->prof[18] = 0ull;
         }
 #endif
         decide_phase<THREADS, CACHE>(s, s_state, s_hist, s_sel);

@@ -101,6 +101,12 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_
             uint32_t const nj = s_state[kStJobs];
             uint32_t const wave = s_state[kStWaves];
             const uint32_t* jobs = s_state[kStInList] ? s.list[cur] : s.jobs;
+#ifdef GHCM_PROFILE
+            if (tid == 0 && blockIdx.x < nj) {  // the latest first-job start of the wave
+                unsigned long long const rel = ld_relaxed_u64(&ctl->release_ns);
+                atomicMax(&ctl->prof[16], static_cast<unsigned long long>(global_ns() - rel));
+            }
+#endif
             for (uint32_t j = blockIdx.x; j < nj; j += gridDim.x) {
                 uint32_t const job = __ldcg(&jobs[j]);
                 if (job >= s.num_tiles) {  // never written by a correct decision: stop the grid
@@ -112,6 +118,12 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_
                 if (r == kJobFailed) break;
                 solves += (r == kJobSolved) ? 1u : 0u;
             }
+#ifdef GHCM_PROFILE
+            if (tid == 0 && blockIdx.x < nj) {  // the latest job end of the wave
+                unsigned long long const rel = ld_relaxed_u64(&ctl->release_ns);
+                atomicMax(&ctl->prof[14], static_cast<unsigned long long>(global_ns() - rel));
+            }
+#endif
             GHCM_PROF_END(ctl, 1, t_solve);
         } else if (phase == kPhaseScore) {
             score_phase<G::THREADS>(s, cur, s_state[kStJobs], s_state[kStWaves] + 1u, s_hist, s_krange);

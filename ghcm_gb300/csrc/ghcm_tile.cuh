@@ -371,6 +371,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         atomicAdd(&s.ctl->prof[11], static_cast<unsigned long long>(p_t2 - p_t1));
         atomicAdd(&s.ctl->prof[12], static_cast<unsigned long long>(p_t3 - p_t2));
         atomicAdd(&s.ctl->prof[13], 1ull);
+        atomicMax(&s.ctl->prof[18], static_cast<unsigned long long>(p_t3 - p_t0));  // longest solve of the wave
         atomicAdd(&s.ctl->prof[3], static_cast<unsigned long long>(sweeps));
         atomicMax(&s.ctl->wave_max_sweeps, sweeps);
     }
