@@ -82,7 +82,7 @@ __device__ __forceinline__ void activate(const Sched& s, uint32_t tile, uint32_t
         atomicMin(&s_krange[0], kb);
         atomicMax(&s_krange[1], kb);
     }
-    uint32_t const old = atomicOr(&s.flags[tile], kActive | bits);
+    uint32_t const old = atom_or_release(&s.flags[tile], kActive | bits);
     if (!(old & kActive)) {
         uint32_t const pos = atomicAdd(&s.ctl->count[nxt], 1u);
         if (pos < s.num_tiles)
@@ -445,13 +445,11 @@ __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, 
         }
         s_krange[0] = inf_bits();
         s_krange[1] = 0u;
-        __threadfence();  // publish this CTA's work
-        uint32_t const arrived = atomicAdd(&ctl->bar_count, 1u) + 1u;
+        // publish this CTA's work (gathered by the barrier above) and, for the
+        // last to arrive, acquire everyone's
+        uint32_t const arrived = atom_add_acq_rel(&ctl->bar_count, 1u) + 1u;
         s_last = (arrived == gridDim.x) ? 1u : 0u;
-        if (s_last) {
-            __threadfence();  // acquire everyone's work
-            ctl->bar_count = 0u;
-        }
+        if (s_last) ctl->bar_count = 0u;
     }
     __syncthreads();
     if (s_last) {
@@ -479,8 +477,7 @@ __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, 
             ctl->prof[9] += 1u;
             ctl->release_ns = t_rel;
 #endif
-            __threadfence();
-            st_release_u64(&ctl->release, w);
+            st_release_u64(&ctl->release, w);  // the decision's stores, gathered by the barrier above
             unpack_release(w, s_state);
         }
     } else if (threadIdx.x == 0) {

@@ -85,10 +85,9 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     // Claim: clear the tile's activation state (a later activation re-queues
     // it), then stage the tile with its halo.
     if (tid == 0) {
-        uint32_t const f = atomicAnd(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
+        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
         uint32_t const kold = atomicExch(&s.key[tile], inf_bits());
         uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
-        __threadfence();
         s_word[0] = f;
         s_word[1] = 0u;  // abort flag
         s_word[4] = 0u;  // edge rows changed by this solve
@@ -346,22 +345,17 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     for (int o = 16; o >= 1; o >>= 1) lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
     if ((tid & 31) == 0) s_red[tid >> 5] = lmin;
     __syncthreads();
-    // an activating thread fences once: the barrier above has made every
-    // thread's tile stores visible to it, the fence orders them before its
-    // activation (cumulativity), so the neighbour's stage sees them
+    // the barrier above gathers every thread's tile stores; an activation is a
+    // release, so the neighbour that consumes it stages them
     if (tid == 0) {
         float m = s_red[0];
         for (int w = 1; w < G::THREADS / 32; ++w) m = fminf(m, s_red[w]);
         s.tmin[tile] = m;
         learn_commit(s, tile, useful, wave, sweeps, sm.feat);
-        if (capped) {
-            __threadfence();
-            activate(s, tile, kFull, m, nxt, s_krange);
-        }
+        if (capped) activate(s, tile, kFull, m, nxt, s_krange);
     }
     uint32_t const edge_changed = s_word[4];
     if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u)) {
-        __threadfence();
         activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt, s_krange);
     }
 #ifdef GHCM_PROFILE

@@ -57,13 +57,12 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
 
     // Claim and stage.
     if (lane == 0) {
-        uint32_t const f = atomicAnd(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
+        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
         uint32_t const kold = atomicExch(&s.key[tile], inf_bits());
         uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
         sm.claim[0] = f;
         sm.claim[1] = kold;
         sm.claim[2] = kmx;
-        __threadfence();
         if (use_tma) {
             fence_proxy_async();
             mbar_arrive_expect_tx(&sm.bar, static_cast<uint32_t>(2 * G::BOX * sizeof(float)));
@@ -234,7 +233,6 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     capped = __any_sync(FULL, capped);
     __syncwarp();
     if (lane == 0) {
-        __threadfence();  // the warp's tile stores before its activations
         s.tmin[tile] = lmin;
         learn_commit(s, tile, useful, wave, sweeps, sm.feat);
 #pragma unroll
