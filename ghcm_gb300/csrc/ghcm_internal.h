@@ -52,7 +52,6 @@ struct Ctl {
     uint32_t krange[2][2];         // per list: {min, max} key bits of its tiles (a superset range)
     float    wave_front;           // smallest key of the set being scheduled this wave
     float    wave_span;            // its key range (max - min, > 0)
-    uint32_t take_count;           // learned schedule: tiles the score phase took
     uint32_t trace_count;          // trace records written (may exceed the capacity)
     uint32_t score_waves;          // learned schedule: waves chosen by score
     uint32_t fallback_waves;       // learned schedule: waves that fell back to the plain top-n
@@ -95,6 +94,8 @@ struct Learn {
     uint32_t* nsolve;      // per tile: block-solves so far
     uint32_t* last_change; // per tile: wave of its last useful solve + 1 (0: none)
     uint32_t* vetoes;      // per tile: consecutive vetoes (veto mode)
+    float*    score;       // per tile: model logit, written by the solve that queued it (score mode)
+    uint32_t* score_tag;   // per tile: 1 while score[] belongs to the tile's current activation
     const float* params;   // MLP parameters (kParams floats); nullptr: plain schedule
     TraceRec* trace;       // trace records; nullptr: no trace
     uint32_t  trace_cap;

@@ -1,12 +1,12 @@
 // Learned block schedule: per-tile features, the warp-cooperative MLP that
-// scores a tile, and the score phase that partitions an active set by score.
+// scores a tile as it is queued, and the claim-time veto.
 //
 // The reference picks the n tiles with the smallest frozen min-time key
 // (src/eikonal_hcm.cpp:47-80, 344-358). The learned schedule scores every
-// active tile with a 12 -> 64 -> 64 -> 1 FP32 MLP estimating P(the solve moves
-// some cell by more than eps) and solves those scoring at or above a
-// threshold (tiles re-queued by the residual judge or a sweep cap always
-// go); if none qualifies it falls back to the plain top-n. The global Godunov
+// active tile with a 12 -> 64 -> 64 -> 1 FP32 MLP (the CTA that queues a tile
+// scores it right after its own solve) and solves those scoring at or above a
+// threshold (tiles re-queued by the residual judge or a sweep cap always go),
+// filled up to fallback_jobs in the plain key order. The global Godunov
 // residual judge is unchanged, so a wrong score costs work, never accuracy.
 //
 // The same features are written, with the outcome of each solve, by the
@@ -62,40 +62,46 @@ __device__ __forceinline__ void tile_features(const Sched& s, uint32_t tile, uin
     f[11] = 0.25f * static_cast<float>(__popc((flags & kEdgeMask) >> 4));
 }
 
+// The MLP parameters staged in the kernel's dynamic shared memory (kParams
+// floats) by every CTA of a learned-schedule launch, so that scoring reads
+// them at shared-memory latency.
+extern __shared__ __align__(16) float g_mlp_params[];
+
 // Logit of the MLP for features x, computed by the whole warp (every lane
-// holds x and gets the result). Lane l owns hidden units l and l + 32.
+// holds x and gets the result). Lane l owns hidden units l and l + 32. P is
+// the flat parameter vector (shared or global memory).
 __device__ __forceinline__ float mlp_logit_warp(const float* __restrict__ P, const float (&x)[kFeatures]) {
     constexpr unsigned FULL = 0xffffffffu;
     int const lane = threadIdx.x & 31;
-    float h0 = __ldg(&P[kOffB1 + lane]);
-    float h1 = __ldg(&P[kOffB1 + 32 + lane]);
+    float h0 = (P[kOffB1 + lane]);
+    float h1 = (P[kOffB1 + 32 + lane]);
 #pragma unroll
     for (int i = 0; i < kFeatures; ++i) {
-        h0 = fmaf(__ldg(&P[kOffW1 + i * kHidden + lane]), x[i], h0);
-        h1 = fmaf(__ldg(&P[kOffW1 + i * kHidden + 32 + lane]), x[i], h1);
+        h0 = fmaf((P[kOffW1 + i * kHidden + lane]), x[i], h0);
+        h1 = fmaf((P[kOffW1 + i * kHidden + 32 + lane]), x[i], h1);
     }
     h0 = fmaxf(h0, 0.f);
     h1 = fmaxf(h1, 0.f);
-    float a0 = __ldg(&P[kOffB2 + lane]);
-    float a1 = __ldg(&P[kOffB2 + 32 + lane]);
+    float a0 = (P[kOffB2 + lane]);
+    float a1 = (P[kOffB2 + 32 + lane]);
 #pragma unroll 8
     for (int k = 0; k < 32; ++k) {
         float const v = __shfl_sync(FULL, h0, k);
-        a0 = fmaf(__ldg(&P[kOffW2 + k * kHidden + lane]), v, a0);
-        a1 = fmaf(__ldg(&P[kOffW2 + k * kHidden + 32 + lane]), v, a1);
+        a0 = fmaf((P[kOffW2 + k * kHidden + lane]), v, a0);
+        a1 = fmaf((P[kOffW2 + k * kHidden + 32 + lane]), v, a1);
     }
 #pragma unroll 8
     for (int k = 0; k < 32; ++k) {
         float const v = __shfl_sync(FULL, h1, k);
-        a0 = fmaf(__ldg(&P[kOffW2 + (k + 32) * kHidden + lane]), v, a0);
-        a1 = fmaf(__ldg(&P[kOffW2 + (k + 32) * kHidden + 32 + lane]), v, a1);
+        a0 = fmaf((P[kOffW2 + (k + 32) * kHidden + lane]), v, a0);
+        a1 = fmaf((P[kOffW2 + (k + 32) * kHidden + 32 + lane]), v, a1);
     }
     a0 = fmaxf(a0, 0.f);
     a1 = fmaxf(a1, 0.f);
-    float z = fmaf(__ldg(&P[kOffW3 + lane]), a0, __ldg(&P[kOffW3 + 32 + lane]) * a1);
+    float z = fmaf((P[kOffW3 + lane]), a0, (P[kOffW3 + 32 + lane]) * a1);
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) z += __shfl_xor_sync(FULL, z, o);
-    return z + __ldg(&P[kOffB3]);
+    return z + (P[kOffB3]);
 }
 
 // Per-tile log2 speed statistics (features 4-6), one warp per tile.
@@ -129,80 +135,23 @@ __device__ void tile_speed_stats(const Sched& s, uint32_t tile) {
     }
 }
 
-// Score phase: the CTA's warps score the tiles of list[cur][lo, hi) and
-// partition them - taken tiles to s.jobs (up to max_jobs; the overflow is
-// carried), the rest to list[cur ^ 1]. Per round each warp scores one tile;
-// the CTA then reserves its slots with one atomic per list. Carried keys
-// widen s_krange (the key range of list[cur ^ 1]).
-template <int THREADS>
-__device__ void score_phase(const Sched& s, uint32_t cur, uint32_t m, uint32_t wave, uint32_t* s_buf,
-                            uint32_t* s_krange) {
-    constexpr int NW = THREADS / 32;
-    int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+// Score policy: the model logit of `tile`, just queued for the next wave by
+// the calling CTA's solve, computed by the calling warp and kept in score[]
+// (score_tag = 1) for the next decision. Tiles re-queued in full need none
+// (they are always taken). A tile queued by two neighbours is scored twice;
+// the later write stands.
+__device__ void score_queued_warp(const Sched& s, uint32_t tile, uint32_t wave) {
+    uint32_t const flags = ld_relaxed(&s.flags[tile]);
+    if (!(flags & kActive) || (flags & kFull)) return;
     Ctl* ctl = s.ctl;
-    float const front = ld_relaxed_f(&ctl->wave_front);
-    float const span = ld_relaxed_f(&ctl->wave_span);
-    float const thr_logit = logf(s.learn.threshold / (1.f - s.learn.threshold));
-    uint32_t const per = (m + gridDim.x - 1) / gridDim.x;
-    uint32_t const lo = min(m, blockIdx.x * per), hi = min(m, lo + per);
-    // s_buf: [0] take count, [1] carry count, [2] take base, [3] carry base,
-    //        [4, 4+NW) taken tiles, [4+NW, 4+2NW) carried tiles
-    for (uint32_t base = lo; base < hi; base += NW) {
-        if (threadIdx.x < 2) s_buf[threadIdx.x] = 0u;
-        __syncthreads();
-        uint32_t const j = base + static_cast<uint32_t>(warp);
-        if (j < hi) {
-            uint32_t const tile = __ldcg(&s.list[cur][j]);
-            uint32_t const flags = ld_relaxed(&s.flags[tile]);
-            float const key = __uint_as_float(__ldcg(&s.key[tile]));
-            float const kmax = __uint_as_float(__ldcg(&s.learn.kmax[tile]));
-            float x[kFeatures];
-            tile_features(s, tile, flags, key, kmax, wave, front, span, x);
-            float const z = mlp_logit_warp(s.learn.params, x);
-            if (lane == 0) {
-                if ((flags & kFull) || z >= thr_logit) {
-                    s_buf[4 + atomicAdd(&s_buf[0], 1u)] = tile;
-                } else {
-                    s_buf[4 + NW + atomicAdd(&s_buf[1], 1u)] = tile;
-                    uint32_t const kb = __float_as_uint(key < f_inf() ? key : front + span);
-                    atomicMin(&s_krange[0], kb);
-                    atomicMax(&s_krange[1], kb);
-                }
-            }
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            s_buf[2] = s_buf[0] ? atomicAdd(&ctl->take_count, s_buf[0]) : 0u;
-            s_buf[3] = 0u;
-        }
-        __syncthreads();
-        // taken beyond max_jobs are carried too
-        uint32_t const nt = s_buf[0];
-        uint32_t const tbase = s_buf[2];
-        uint32_t const over = (tbase + nt > s.max_jobs) ? min(nt, tbase + nt - s.max_jobs) : 0u;
-        if (threadIdx.x == 0) {
-            uint32_t const nc = s_buf[1] + over;
-            s_buf[3] = nc ? atomicAdd(&ctl->count[cur ^ 1u], nc) : 0u;
-        }
-        __syncthreads();
-        if (threadIdx.x < nt) {
-            uint32_t const t = s_buf[4 + threadIdx.x];
-            uint32_t const pos = tbase + threadIdx.x;
-            if (pos < s.max_jobs) {
-                s.jobs[pos] = t;
-            } else {
-                uint32_t const at = s_buf[3] + s_buf[1] + (pos - max(tbase, s.max_jobs));
-                s.list[cur ^ 1u][at] = t;
-                float const key = __uint_as_float(__ldcg(&s.key[t]));
-                uint32_t const kb = __float_as_uint(key < f_inf() ? key : front + span);
-                atomicMin(&s_krange[0], kb);
-                atomicMax(&s_krange[1], kb);
-            }
-        } else if (threadIdx.x >= 32 && threadIdx.x - 32 < s_buf[1]) {
-            uint32_t const q = threadIdx.x - 32;
-            s.list[cur ^ 1u][s_buf[3] + q] = s_buf[4 + NW + q];
-        }
-        __syncthreads();
+    float const key = __uint_as_float(__ldcg(&s.key[tile]));
+    float const kmax = __uint_as_float(__ldcg(&s.learn.kmax[tile]));
+    float x[kFeatures];
+    tile_features(s, tile, flags, key, kmax, wave, ld_relaxed_f(&ctl->wave_front), ld_relaxed_f(&ctl->wave_span), x);
+    float const z = mlp_logit_warp(g_mlp_params, x);
+    if ((threadIdx.x & 31) == 0) {
+        __stcg(&s.learn.score[tile], z);
+        __stcg(&s.learn.score_tag[tile], 1u);
     }
 }
 
@@ -217,6 +166,7 @@ __device__ __forceinline__ uint32_t learn_claim(const Sched& s, uint32_t tile, u
                                                 uint32_t wave, float* feat) {
     if (!s.learn.tstat) return 0u;
     uint32_t const kmx = atomicExch(&s.learn.kmax[tile], 0u);
+    if (s.learn.score_tag) __stcg(&s.learn.score_tag[tile], 0u);  // its score belonged to this activation
     if (s.learn.trace) {
         float f[kFeatures];
         tile_features(s, tile, flags, __uint_as_float(key_bits), __uint_as_float(kmx), wave,
@@ -238,7 +188,7 @@ __device__ __forceinline__ bool learn_veto_warp(const Sched& s, uint32_t tile, u
     float x[kFeatures];
     tile_features(s, tile, flags, __uint_as_float(key_bits), __uint_as_float(kmax_bits), wave,
                   ld_relaxed_f(&s.ctl->wave_front), ld_relaxed_f(&s.ctl->wave_span), x);
-    float const z = mlp_logit_warp(s.learn.params, x);
+    float const z = mlp_logit_warp(g_mlp_params, x);
     return z < logf(s.learn.threshold / (1.f - s.learn.threshold));
 }
 

@@ -15,7 +15,6 @@ enum : uint32_t {
     kPhaseResidual = 2,  // global fixed-point check
     kPhaseDone = 3,
     kPhaseStop = 4,
-    kPhaseScore = 5,     // learned schedule: score and partition the active set
 };
 
 struct TileCoord {
@@ -72,8 +71,9 @@ __device__ __forceinline__ float to_cost(const Inst& I, float v) {
 // into its flags and appends it to list[nxt] unless it is already active.
 // The device form of the dirty-set test + heap push + border-mask OR of
 // src/eikonal_hcm.cpp:451-462. s_krange (the calling CTA's {min, max} key
-// bits of what it activated this phase) is widened to `key`.
-__device__ __forceinline__ void activate(const Sched& s, uint32_t tile, uint32_t bits, float key, uint32_t nxt,
+// bits of what it activated this phase) is widened to `key`. Returns true
+// when this call appended the tile (it was idle).
+__device__ __forceinline__ bool activate(const Sched& s, uint32_t tile, uint32_t bits, float key, uint32_t nxt,
                                          uint32_t* s_krange) {
     uint32_t const kb = __float_as_uint(key);
     atomicMin(&s.key[tile], kb);
@@ -89,7 +89,9 @@ __device__ __forceinline__ void activate(const Sched& s, uint32_t tile, uint32_t
             s.list[nxt][pos] = tile;
         else
             atomicOr(&s.ctl->error, kErrInternal);
+        return true;
     }
+    return false;
 }
 
 // Priority key of an active tile (smaller = solved first), as float bits.
@@ -324,17 +326,86 @@ __device__ void plan_plain_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t
     }
 }
 
+// Learned schedule, score policy: the tiles of list[act] (m) re-queued in full
+// or whose score (written when they were queued) reaches the threshold become
+// jobs (at most max_jobs), the rest are carried to list[act ^ 1]; if fewer
+// than fallback_jobs were taken the wave is filled from the carried tiles in
+// plain key order. Returns the list the JOBS phase treats as current (its
+// activations go to the other one). Counters and s_sel[8], [11] as in
+// plan_plain_jobs.
+template <int THREADS, int CACHE>
+__device__ uint32_t plan_learned_jobs(const Sched& s, uint32_t act, uint32_t m, float lo, float hi, uint32_t* s_hist,
+                                      uint32_t* s_sel) {
+    Ctl* ctl = s.ctl;
+    int const tid = threadIdx.x;
+    float const thr = logf(s.learn.threshold / (1.f - s.learn.threshold));
+    uint32_t const cap = s.max_jobs;
+    if (tid == 0) {
+        s_sel[6] = 0u;  // taken
+        s_sel[7] = 0u;  // carried
+    }
+    __syncthreads();
+    auto place = [&](uint32_t t, bool take) {
+        if (take) {
+            uint32_t const pos = atomicAdd(&s_sel[6], 1u);
+            if (pos < cap)
+                s.jobs[pos] = t;
+            else
+                take = false;
+        }
+        if (!take) s.list[act ^ 1u][atomicAdd(&s_sel[7], 1u)] = t;
+    };
+    uint32_t i = tid;
+    for (; i + 3u * THREADS < m; i += 4u * THREADS) {  // four entries in flight per thread
+        uint32_t t4[4], f4[4], g4[4];
+        float z4[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) t4[u] = __ldcg(&s.list[act][i + u * THREADS]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            f4[u] = ld_relaxed(&s.flags[t4[u]]);
+            g4[u] = __ldcg(&s.learn.score_tag[t4[u]]);
+            z4[u] = __ldcg(&s.learn.score[t4[u]]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) place(t4[u], (f4[u] & kFull) || (g4[u] != 0u && z4[u] >= thr));
+    }
+    for (; i < m; i += THREADS) {
+        uint32_t const t = __ldcg(&s.list[act][i]);
+        place(t, (ld_relaxed(&s.flags[t]) & kFull) ||
+                     (__ldcg(&s.learn.score_tag[t]) != 0u && __ldcg(&s.learn.score[t]) >= thr));
+    }
+    __syncthreads();
+    uint32_t const take = min(s_sel[6], cap);
+    uint32_t const carried = s_sel[7];
+    uint32_t const want = min(s.learn.fallback_jobs, cap);
+    __syncthreads();  // s_sel[6..7] are read before the select reuses s_sel
+    if (take >= want || carried == 0u) {
+        if (tid == 0) {
+            ctl->count[act ^ 1u] = carried;
+            ctl->krange[act ^ 1u][0] = carried ? __float_as_uint(lo) : inf_bits();
+            ctl->krange[act ^ 1u][1] = carried ? __float_as_uint(hi) : 0u;
+            s_sel[8] = 0u;
+            s_sel[11] = take;
+            atomicAdd(take ? &ctl->score_waves : &ctl->fallback_waves, 1u);
+        }
+        return act;
+    }
+    plan_plain_jobs<THREADS, CACHE>(s, act ^ 1u, carried, want - take, take, lo, hi, s_hist, s_sel);
+    if (tid == 0) atomicAdd(take ? &ctl->score_waves : &ctl->fallback_waves, 1u);
+    return act ^ 1u;
+}
+
 // Decides the next phase; run by the whole of the last CTA to reach the wave
 // barrier while every other CTA waits. `st` is this CTA's view of the state
 // the previous barrier published. Returns the new
 // {jobs-in-list, phase, cur, job count} in s_sel[8..11].
 //   after INIT / JOBS / RESIDUAL, the set to process is list[act]:
 //     non-empty, plain        -> JOBS on its n lowest keys (the rest carried over)
-//     non-empty, learned      -> SCORE: partition it by the model's score
+//     non-empty, learned      -> JOBS on the tiles whose score qualifies,
+//                                filled up to fallback_jobs in plain key order
 //     empty after JOBS        -> RESIDUAL: the global fixed-point check
 //     empty after RESIDUAL    -> DONE
-//   after SCORE: JOBS on the tiles it took, filled up to fallback_jobs from
-//   the carried set in plain key order (all of the wave when it took none).
 // The key range of list[act] comes from the activations (ctl->krange); its
 // min and span are published as this wave's front for the features.
 template <int THREADS, int CACHE>
@@ -344,29 +415,7 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
     uint32_t const prev = st[kStPhase];
     uint32_t const cur = st[kStCur];
     uint32_t phase = kPhaseJobs, ncur = cur;
-    if (prev == kPhaseScore) {
-        // the score phase took `take` tiles into jobs[0, take) and carried the
-        // rest to list[L]; fill the wave up to fallback_jobs from list[L] in
-        // plain key order
-        uint32_t const L = cur ^ 1u;
-        uint32_t const take = min(ld_relaxed(&ctl->take_count), s.max_jobs);
-        uint32_t const want = min(s.learn.fallback_jobs, s.max_jobs);
-        uint32_t const m = ld_relaxed(&ctl->count[L]);
-        if (take >= want || m == 0u) {
-            if (tid == 0) {
-                s_sel[8] = 0u;
-                s_sel[11] = take;
-                atomicAdd(&ctl->score_waves, 1u);
-            }
-        } else {
-            float const lo = __uint_as_float(ld_relaxed(&ctl->krange[L][0]));
-            float const hi = __uint_as_float(ld_relaxed(&ctl->krange[L][1]));
-            plan_plain_jobs<THREADS, CACHE>(s, L, m, want - take, take, lo, hi, s_hist, s_sel);
-            ncur = L;
-            if (tid == 0) atomicAdd(take ? &ctl->score_waves : &ctl->fallback_waves, 1u);
-        }
-        if (tid == 0) atomicAdd(&ctl->waves, 1u);
-    } else {
+    {
         uint32_t const act = (prev == kPhaseInit) ? 0u : (cur ^ 1u);
         uint32_t const m = ld_relaxed(&ctl->count[act]);
         if (m == 0u) {
@@ -402,20 +451,11 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
                 atomicMax(&ctl->max_active, m);
             }
             ncur = act;
-            if (s.learn.params && !s.learn.veto) {
-                phase = kPhaseScore;  // carries and activations go to list[act ^ 1]
-                if (tid == 0) {
-                    ctl->count[act ^ 1u] = 0u;
-                    ctl->krange[act ^ 1u][0] = inf_bits();
-                    ctl->krange[act ^ 1u][1] = 0u;
-                    ctl->take_count = 0u;
-                    s_sel[8] = 1u;
-                    s_sel[11] = m;  // tiles to score
-                }
-            } else {
+            if (s.learn.params && !s.learn.veto)
+                ncur = plan_learned_jobs<THREADS, CACHE>(s, act, m, lo, hi, s_hist, s_sel);
+            else
                 plan_plain_jobs<THREADS, CACHE>(s, act, m, s.max_jobs, 0u, lo, hi, s_hist, s_sel);
-                if (tid == 0) atomicAdd(&ctl->waves, 1u);
-            }
+            if (tid == 0) atomicAdd(&ctl->waves, 1u);
         }
     }
     if (tid == 0) {

@@ -81,6 +81,8 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_
         s_krange[0] = inf_bits();  // keys this CTA activates in a phase: {min, max}
         s_krange[1] = 0u;
     }
+    if (s.learn.params)  // learned schedule: the model in shared memory for scoring
+        for (int i = tid; i < kParams; i += G::THREADS) g_mlp_params[i] = __ldg(&s.learn.params[i]);
     __syncthreads();
     GHCM_PROF_BEGIN(t_kernel);
     uint32_t parity = 0u;
@@ -125,8 +127,6 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_
             }
 #endif
             GHCM_PROF_END(ctl, 1, t_solve);
-        } else if (phase == kPhaseScore) {
-            score_phase<G::THREADS>(s, cur, s_state[kStJobs], s_state[kStWaves] + 1u, s_hist, s_krange);
         } else if (phase == kPhaseResidual) {
             GHCM_PROF_BEGIN(t_res);
             residual_warp<B>(s, cur ^ 1u, gw, nwarps, s_krange);
@@ -166,6 +166,8 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
         s_krange[0] = inf_bits();
         s_krange[1] = 0u;
     }
+    if (s.learn.params)
+        for (int i = tid; i < kParams; i += W::THREADS) g_mlp_params[i] = __ldg(&s.learn.params[i]);
     __syncthreads();
     GHCM_PROF_BEGIN(t_kernel);
     uint32_t parity = 0u;
@@ -196,8 +198,6 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
                 solves += (r == kJobSolved) ? 1u : 0u;
             }
             GHCM_PROF_END(ctl, 1, t_solve);
-        } else if (phase == kPhaseScore) {
-            score_phase<W::THREADS>(s, cur, s_state[kStJobs], s_state[kStWaves] + 1u, s_hist, s_krange);
         } else if (phase == kPhaseResidual) {
             GHCM_PROF_BEGIN(t_res);
             residual_warp<B>(s, cur ^ 1u, gw, nwarps, s_krange);
@@ -236,6 +236,7 @@ __global__ void k_init_inst(Sched s) {
             s.learn.nsolve[g] = 0u;
             s.learn.last_change[g] = 0u;
             s.learn.vetoes[g] = 0u;
+            s.learn.score_tag[g] = 0u;
         }
     }
     size_t const n = static_cast<size_t>(I.w) * I.h;
@@ -382,12 +383,25 @@ cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cuda
     void* k = select_kernel(block, fim);
     if (!k) return cudaErrorInvalidValue;
     void* args[] = {const_cast<Sched*>(&s)};
+    // A learned-schedule launch stages the model in dynamic shared memory; its
+    // grid is capped at what stays co-resident with that.
+    size_t const dyn = s.learn.params ? kParams * sizeof(float) : 0u;
+    if (dyn) {
+        int dev = 0, sms = 0, bps = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, threads_for(block, fim), dyn);
+        if (e != cudaSuccess) return e;
+        if (bps <= 0) return cudaErrorInvalidConfiguration;
+        grid = std::min(grid, bps * sms);
+    }
     // A cooperative launch guarantees the co-residency the grid barrier needs;
     // through cudaLaunchKernelExC it can also be captured into a CUDA graph.
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(threads_for(block, fim));
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = dyn;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

@@ -53,7 +53,10 @@ struct alignas(128) TileSmem {
     float cost[TileGeom<B>::BOXP];
     uint8_t check[B * B];  // block-FIM: re-check requests
     float feat[kFeatures]; // trace recorder: features of the current solve
+    uint32_t queued[4];    // learned score policy: neighbour queued across edge e, or kNone
 };
+
+constexpr uint32_t kNone = 0xffffffffu;
 
 // index of local cell (x, y), x in [-4, B+4), y in [-2, B+2), in a staged box
 template <int B>
@@ -92,6 +95,8 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         s_word[1] = 0u;  // abort flag
         s_word[4] = 0u;  // edge rows changed by this solve
         s_word[5] = kold;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) sm.queued[e] = kNone;
         s_word[6] = kmx;
         if (use_tma) {
             fence_proxy_async();
@@ -356,7 +361,13 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     }
     uint32_t const edge_changed = s_word[4];
     if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u)) {
-        activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt, s_krange);
+        if (activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt, s_krange))
+            sm.queued[e] = static_cast<uint32_t>(nb);  // appended now: score it (a re-activation keeps its score)
+    }
+    if (s.learn.params && !s.learn.veto) {  // score policy: score what this solve queued, a warp per tile
+        __syncthreads();
+        for (int q = tid >> 5; q < 4; q += G::THREADS / 32)
+            if (sm.queued[q] != kNone) score_queued_warp(s, sm.queued[q], wave + 1u);
     }
 #ifdef GHCM_PROFILE
     if (tid == 0) {

@@ -176,9 +176,10 @@ POLICY_VETO = _lib.GHCM_POLICY_VETO
 
 
 def set_policy(setup, policy: int = POLICY_SCORE, max_vetoes: int = 2) -> None:
-    """How the model is used: POLICY_SCORE (the default: a score phase picks
-    the wave, filled up to fallback_jobs in key order) or POLICY_VETO (the
-    plain top-n proposes, the model defers low-scoring claims)."""
+    """How the model is used: POLICY_SCORE (the default: each tile is scored by
+    the solve that queues it; a wave takes those at or above the threshold
+    and is filled up to fallback_jobs in key order) or POLICY_VETO (the plain
+    top-n proposes, the model defers low-scoring claims)."""
     rc = _lib.load().ghcm_set_schedule_policy(setup.handle, int(policy), int(max_vetoes))
     if rc != 0:
         raise GhcmError(rc, "ghcm_set_schedule_policy")

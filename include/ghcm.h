@@ -244,9 +244,11 @@ int ghcm_trace_read(ghcm_ctx* ctx, ghcm_trace_record* out, uint32_t max_records,
 int ghcm_set_schedule_model(ghcm_ctx* ctx, const float* params, uint32_t n_params, float threshold);
 
 /* How the learned schedule uses the model:
- *   GHCM_POLICY_SCORE (default): a score phase before every wave scores the whole active
- *     set; the wave solves the tiles at or above the threshold, filled up to
- *     cfg.fallback_jobs tiles in plain key order.
+ *   GHCM_POLICY_SCORE (default): the CTA that queues a tile for the next wave
+ *     scores it right after its own solve; the next wave solves the tiles
+ *     scoring at or above the threshold, filled up to cfg.fallback_jobs tiles
+ *     in plain key order (tiles queued without a score - the seeds' and, at
+ *     block_size 8, every tile - go by key).
  *   GHCM_POLICY_VETO: the plain top-n proposes the wave; a CTA that
  *     claims a tile scores it first and defers it (back into the active set,
  *     key and edge bits kept) when the score is below the threshold, at most

@@ -188,8 +188,9 @@ def test_learned_schedule_keeps_parity(dev, oracle_lib, trained, block, policy):
         c = learned.counters(s)
     assert rel_diff(res.field, ref) <= TOL and np.all(res.field[seeds[:, 1], seeds[:, 0]] == 0.0)
     if policy == learned.POLICY_SCORE:
-        assert c["score_waves"] + c["fallback_waves"] == res.stats["waves"] and c["score_waves"] > 0
-        assert c["vetoes"] == 0
+        assert c["score_waves"] + c["fallback_waves"] == res.stats["waves"] and c["vetoes"] == 0
+        if block != 8:  # one warp per tile at block 8 queues tiles unscored: those waves go by key
+            assert c["score_waves"] > c["fallback_waves"]
     else:
         assert c["score_waves"] == 0 and c["fallback_waves"] == 0
 
@@ -215,10 +216,10 @@ def test_extreme_models(dev, oracle_lib, bias, policy):
             assert c["vetoes"] >= res.stats["block_solves"] // 2
         else:
             assert c["vetoes"] == 0
-    elif bias < 0:
+    elif bias < 0:  # nothing qualifies: every wave is filled in key order
         assert c["fallback_waves"] > 0
-    else:
-        assert c["fallback_waves"] == 0
+    else:  # every scored tile qualifies; only the first wave (the seeds', queued unscored) goes by key
+        assert c["fallback_waves"] <= 2 and c["score_waves"] > c["fallback_waves"]
 
 
 def test_learned_batch(dev, oracle_lib, trained):
