@@ -176,24 +176,7 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     ctx->counters[1] = c.fallback_waves;
     ctx->counters[2] = c.trace_count;
     ctx->counters[3] = c.vetoes;
-#ifdef GHCM_PROFILE
-    std::fprintf(stderr,
-                 "[ghcm-prof] grid %d solves %llu waves %u residual_passes %u kernel_us %.1f | per wave: "
-                 "decide %.2f us, span %.2f us, release seen after %.2f us, max sweeps %.1f | sweeps/solve %.1f\n",
-                 grid, c.block_solves, c.waves, c.residual_passes, c.prof[5] / 1e3,
-                 c.prof[2] / 1e3 / std::max(1ull, c.prof[9]), c.prof[6] / 1e3 / std::max(1ull, c.prof[9]),
-                 c.prof[7] / 1e3 / std::max(1ull, c.prof[9]) / std::max(1, grid - 1),
-                 double(c.prof[8]) / std::max(1ull, c.prof[9]), double(c.prof[3]) / std::max(1ull, c.block_solves));
-    if (c.prof[9])
-        std::fprintf(stderr, "[ghcm-prof] per wave, after the release: latest first-job start %.2f us, latest job end "
-                     "%.2f us, longest block-solve %.2f us\n",
-                     c.prof[17] / 1e3 / c.prof[9], c.prof[15] / 1e3 / c.prof[9], c.prof[19] / 1e3 / c.prof[9]);
-    if (c.prof[13])
-        std::fprintf(stderr, "[ghcm-prof] per CTA block-solve: stage %.2f us, sweeps %.2f us (%.3f us/sweep), "
-                     "probe+commit+activate %.2f us\n",
-                     c.prof[10] / 1e3 / c.prof[13], c.prof[11] / 1e3 / c.prof[13],
-                     c.prof[11] / 1e3 / std::max(1ull, c.prof[3]), c.prof[12] / 1e3 / c.prof[13]);
-#endif
+    print_profile(c, grid);
     if (stats) {
         float ms = 0.f, kms = 0.f;
         cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);

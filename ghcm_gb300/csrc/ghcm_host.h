@@ -7,7 +7,9 @@
 #include "ghcm_internal.h"
 
 #include <cstddef>
+#include <algorithm>
 #include <cstdint>
+#include <cstdio>
 
 namespace ghcm {
 
@@ -84,6 +86,31 @@ inline uint32_t bytes_per_solve(uint32_t b) { return 4u * b * b + 4u * ((b + 2u)
 // The cost cap of a config (+inf when off).
 inline float cost_cap_of(const ghcm_config& cfg) {
     return cfg.cost_cap > 0.f ? cfg.cost_cap : __builtin_huge_valf();
+}
+
+// GHCM_PROFILE builds: the per-phase counters of a finished solve, on stderr.
+inline void print_profile(const Ctl& c, int grid) {
+#ifdef GHCM_PROFILE
+    std::fprintf(stderr,
+                 "[ghcm-prof] grid %d solves %llu waves %u residual_passes %u kernel_us %.1f | per wave: "
+                 "decide %.2f us, span %.2f us, release seen after %.2f us, max sweeps %.1f | sweeps/solve %.1f\n",
+                 grid, c.block_solves, c.waves, c.residual_passes, c.prof[5] / 1e3,
+                 c.prof[2] / 1e3 / std::max(1ull, c.prof[9]), c.prof[6] / 1e3 / std::max(1ull, c.prof[9]),
+                 c.prof[7] / 1e3 / std::max(1ull, c.prof[9]) / std::max(1, grid - 1),
+                 double(c.prof[8]) / std::max(1ull, c.prof[9]), double(c.prof[3]) / std::max(1ull, c.block_solves));
+    if (c.prof[9])
+        std::fprintf(stderr, "[ghcm-prof] per wave, after the release: latest first-job start %.2f us, latest job end "
+                     "%.2f us, longest block-solve %.2f us\n",
+                     c.prof[17] / 1e3 / c.prof[9], c.prof[15] / 1e3 / c.prof[9], c.prof[19] / 1e3 / c.prof[9]);
+    if (c.prof[13])
+        std::fprintf(stderr, "[ghcm-prof] per CTA block-solve: stage %.2f us, sweeps %.2f us (%.3f us/sweep), "
+                     "probe+commit+activate %.2f us\n",
+                     c.prof[10] / 1e3 / c.prof[13], c.prof[11] / 1e3 / c.prof[13],
+                     c.prof[11] / 1e3 / std::max(1ull, c.prof[3]), c.prof[12] / 1e3 / c.prof[13]);
+#else
+    (void)c;
+    (void)grid;
+#endif
 }
 
 // Scheduler parameters of a config on a device with `sms` SMs.

@@ -253,7 +253,17 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
             if (i < m) place(__ldcg(&list[i]), ck[u]);
         }
     } else {
-        for (uint32_t i = tid; i < m; i += THREADS) {
+        uint32_t i = tid;
+        for (; i + 3u * THREADS < m; i += 4u * THREADS) {  // four entries in flight per thread
+            uint32_t t4[4], k4[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) t4[u] = __ldcg(&list[i + u * THREADS]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) k4[u] = tile_key(s, t4[u]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) place(t4[u], k4[u]);
+        }
+        for (; i < m; i += THREADS) {
             uint32_t const t = __ldcg(&list[i]);
             place(t, tile_key(s, t));
         }
