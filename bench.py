@@ -274,7 +274,31 @@ def timed_device_solves(g, setup, d_speed, d_seeds, d_time, stream, flush, steps
     return sum(a.elapsed_time(b) for a, b in evs) / steps, sts
 
 
-def learned_vs_plain(g, dev, stream, flush, steps: int, warmup: int) -> dict:
+def small_ring_check(g) -> dict:
+    """The configuration the reference runs on the CPU: the 256 x 256 seven-ring
+    field (radii 16..120, width 4, speed 0.01, 8-cell gaps, centre source),
+    solved by gHCM with tiles of 8 and n = 64, against the reference FIM and
+    FMM and the FP64 FMM."""
+    from ghcm_gb300 import fields
+    from oracle.oracle import Oracle, build, rel_diff
+
+    build(with_reference=False)
+    o = Oracle()
+    speed, seeds = fields.ring7_small(seed=1)
+    cost = fields.cost_from_speed(speed)
+    with g.HcmSetup(g.HcmConfig(block_size=8, max_jobs=64, fim_minimum_change=EPS)) as s:
+        res = g.eikonal_hcm_cuda_ex(s, speed, seeds, input_is_speed=True)
+    fim, us_fim = o.fim(cost, seeds, EPS)
+    fmm, us_fmm = o.fmm(cost, seeds)
+    ref64, _ = o.fmm64(cost, seeds)
+    return {"workload": "ring7_256x256", "block": 8, "n": 64, "block_solves": res.stats["block_solves"],
+            "waves": res.stats["waves"], "device_ms": res.stats["device_ms"], "cpu_fim_ms": us_fim / 1e3,
+            "cpu_fmm_ms": us_fmm / 1e3, "max_rel_vs_fim": rel_diff(res.field, fim),
+            "max_rel_vs_fmm": rel_diff(res.field, fmm), "vs_fmm64": fmm64_errors(res.field, ref64),
+            "fim_vs_fmm64": fmm64_errors(fim, ref64)}
+
+
+def learned_vs_plain(g, dev, stream, flush, steps: int, warmup: int, fp64: bool = True) -> dict:
     """The learned schedule against the plain one on the 4096^2 noise field
     (16 sources, seed NOISE_EVAL_SEED, not among the model's training seeds)."""
     import torch
@@ -311,9 +335,17 @@ def learned_vs_plain(g, dev, stream, flush, steps: int, warmup: int) -> dict:
                      "block_solves": statistics.mean(x["block_solves"] for x in sts),
                      "waves": statistics.mean(x["waves"] for x in sts), **c}
     base = out["plain_n1024"]["block_solves"]
+    ref64 = None
+    if fp64:  # the accuracy oracle: FMM in FP64 (checker only)
+        from oracle.oracle import Oracle, build
+
+        build(with_reference=False)
+        ref64, _ = Oracle().fmm64(fields.cost_from_speed(speed), seeds)
     for name in runs:
         out[name]["solves_vs_plain_n1024"] = out[name]["block_solves"] / base
         out[name]["max_rel_vs_plain_n1024"] = rel_diff(fields_out[name], fields_out["plain_n1024"])
+        if ref64 is not None:
+            out[name]["vs_fmm64"] = fmm64_errors(fields_out[name], ref64)
     return {"workload": "noise_4096x4096_16src", "seed": NOISE_EVAL_SEED, "threshold": threshold,
             "model": MODEL.name, "train_seeds": int(len(meta.get("train_seeds", []))), "runs": out}
 
@@ -436,6 +468,14 @@ def run_batched(args, world, rank, local) -> int:
             ref = o.fim(fields.cost_from_speed(inst.speed), inst.seeds, EPS)[0]
             worst = max(worst, rel_diff(dinst[k].d_time.cpu().numpy(), ref))
         line["check"] = {"max_rel_vs_fim_sample": worst, "sample": "every len/8-th instance of rank 0"}
+        # FP64 accuracy on a few instances of each kind
+        errs = []
+        for k in range(0, len(insts), max(1, len(insts) // 6)):
+            inst = insts[k]
+            ref64, _ = o.fmm64(fields.cost_from_speed(inst.speed), inst.seeds)
+            e = fmm64_errors(dinst[k].d_time.cpu().numpy(), ref64)
+            errs.append({"kind": inst.kind, "side": int(inst.speed.shape[0]), **e})
+        line["check"]["vs_fmm64_sample"] = errs
         if not args.no_cpu_baseline:
             sample = all_insts[::8]
             threads = max(1, os.cpu_count() or 1)
@@ -717,7 +757,10 @@ def main() -> int:
             line["check"]["vs_fmm64"] = fmm64_errors(field, ref64)
             line["check"]["fim_vs_fmm64"] = fmm64_errors(fim, ref64)
         if not args.no_learned:
-            line["learned_vs_plain"] = learned_vs_plain(g, dev, stream, flush, max(1, min(args.steps, 3)), 1)
+            line["learned_vs_plain"] = learned_vs_plain(g, dev, stream, flush, max(1, min(args.steps, 3)), 1,
+                                                        fp64=not args.no_cpu_baseline)
+        if not args.no_cpu_baseline:
+            line["small_ring_256"] = small_ring_check(g)
         print(json.dumps(line), flush=True)
     setup.close()
     if dist is not None:
