@@ -36,6 +36,7 @@ EXPORTS = (
     "ghcm_status_string",
     "ghcm_abi_version",
     "ghcm_selftest_wait_timeout",
+    "ghcm_selftest_sqrt",
     "ghcm_solve_device_noalloc",
     "ghcm_batch_create",
     "ghcm_batch_run",
@@ -202,6 +203,7 @@ def load(path: Path | None = None):
     lib.ghcm_status_string.restype = ctypes.c_char_p
     lib.ghcm_abi_version.argtypes = []
     lib.ghcm_selftest_wait_timeout.argtypes = [vp, ctypes.c_uint32]
+    lib.ghcm_selftest_sqrt.argtypes = [vp, ctypes.POINTER(ctypes.c_ulonglong)]
     lib.ghcm_solve_device_noalloc.argtypes = [cfgp, vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
                                               vp, ctypes.c_uint32, vp, vp]
     instp = ctypes.POINTER(GhcmInstance)

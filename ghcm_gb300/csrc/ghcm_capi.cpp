@@ -428,4 +428,18 @@ int ghcm_selftest_wait_timeout(ghcm_ctx* ctx, uint32_t timeout_ms) {
     return (host.error & kErrTimeout) ? GHCM_ERR_TIMEOUT : GHCM_OK;
 }
 
+int ghcm_selftest_sqrt(ghcm_ctx* ctx, unsigned long long* mismatches) {
+    if (!ctx || !mismatches) return GHCM_ERR_BAD_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return GHCM_ERR_CUDA;
+    DevBuf buf;
+    if (!buf.reserve(256)) return GHCM_ERR_OOM;
+    unsigned long long* d_count = buf.as<unsigned long long>();
+    cudaError_t e = cudaMemset(d_count, 0, sizeof(*d_count));
+    if (e == cudaSuccess) e = launch_sqrt_selftest(d_count, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(mismatches, d_count, sizeof(*d_count), cudaMemcpyDeviceToHost);
+    buf.release();
+    return e == cudaSuccess ? GHCM_OK : map_cuda(e);
+}
+
 }  // extern "C"

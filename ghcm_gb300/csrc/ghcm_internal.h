@@ -157,5 +157,8 @@ cudaError_t launch_init(const Sched& s, uint32_t n_insts, uint64_t max_cells, ui
                         cudaStream_t st);
 cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cudaStream_t st);
 cudaError_t launch_wait_selftest(uint32_t* flag, Ctl* ctl, uint64_t timeout_ns, cudaStream_t st);
+// Every 32-bit float through the solver's square root and __fsqrt_rn; adds the
+// number of differing results to *mismatches (device memory).
+cudaError_t launch_sqrt_selftest(unsigned long long* mismatches, cudaStream_t st);
 
 }  // namespace ghcm

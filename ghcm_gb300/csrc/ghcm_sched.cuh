@@ -427,7 +427,11 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
     uint32_t phase = kPhaseJobs, ncur = cur;
     {
         uint32_t const act = (prev == kPhaseInit) ? 0u : (cur ^ 1u);
+        // every control word the decision reads, in one round trip
         uint32_t const m = ld_relaxed(&ctl->count[act]);
+        uint32_t const klo = ld_relaxed(&ctl->krange[act][0]);
+        uint32_t const khi = ld_relaxed(&ctl->krange[act][1]);
+        if (tid == 0) s_sel[12] = ld_relaxed(&ctl->error);
         if (m == 0u) {
             if (prev == kPhaseResidual) {
                 phase = kPhaseDone;
@@ -453,8 +457,8 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
                 s_sel[11] = 0u;
             }
         } else {
-            float const lo = __uint_as_float(ld_relaxed(&ctl->krange[act][0]));
-            float const hi = __uint_as_float(ld_relaxed(&ctl->krange[act][1]));
+            float const lo = __uint_as_float(klo);
+            float const hi = __uint_as_float(khi);
             if (tid == 0) {
                 ctl->wave_front = (lo < f_inf()) ? lo : 0.f;
                 ctl->wave_span = (hi > lo && lo < f_inf()) ? hi - lo : 1.f;
@@ -518,7 +522,8 @@ __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, 
         decide_phase<THREADS, CACHE>(s, s_state, s_hist, s_sel);
         __syncthreads();
         if (threadIdx.x == 0) {
-            uint32_t const err = ld_relaxed(&ctl->error);
+            // errors raised before the arrivals, or the wave cap just hit
+            uint32_t const err = s_sel[12] | (s_sel[9] == kPhaseStop ? 1u : 0u);
             unsigned long long const w =
                 pack_release(s_state[kStGen] + 1u, s_sel[9], s_sel[10], s_sel[11], s_sel[8], err);
 #ifdef GHCM_PROFILE

@@ -292,6 +292,18 @@ __global__ void k_wait_selftest(const uint32_t* flag, Ctl* ctl, uint64_t timeout
     }
 }
 
+// Every 32-bit pattern from `base` on (one per thread) through sqrt_rn and
+// through __fsqrt_rn; adds the number of inputs whose results differ (NaN
+// results compare equal) to *mismatches.
+__global__ void k_sqrt_selftest(uint32_t base, unsigned long long* mismatches) {
+    uint32_t const i = base + blockIdx.x * blockDim.x + threadIdx.x;
+    float const a = __uint_as_float(i);
+    float const r = sqrt_rn(a), e = __fsqrt_rn(a);
+    bool const same = __float_as_uint(r) == __float_as_uint(e) || (isnan(r) && isnan(e));
+    int const bad = __syncthreads_count(!same);
+    if (threadIdx.x == 0 && bad) atomicAdd(mismatches, static_cast<unsigned long long>(bad));
+}
+
 // ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
@@ -409,6 +421,13 @@ cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cuda
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelExC(&cfg, k, args);
+}
+
+cudaError_t launch_sqrt_selftest(unsigned long long* mismatches, cudaStream_t st) {
+    constexpr uint32_t kThreads = 256, kPerLaunch = 1u << 28;
+    for (uint64_t base = 0; base < (1ull << 32); base += kPerLaunch)
+        k_sqrt_selftest<<<kPerLaunch / kThreads, kThreads, 0, st>>>(static_cast<uint32_t>(base), mismatches);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_wait_selftest(uint32_t* flag, Ctl* ctl, uint64_t timeout_ns, cudaStream_t st) {

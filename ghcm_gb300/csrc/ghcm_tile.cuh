@@ -88,8 +88,12 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     // Claim: clear the tile's activation state (a later activation re-queues
     // it), then stage the tile with its halo.
     if (tid == 0) {
-        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
+        // Both atomics in flight at once. The key is reset first: an activation
+        // landing between the two leaves a lower key on an idle tile (it is
+        // only a priority), while its data is staged, since the flag clear
+        // acquires it.
         uint32_t const kold = atomicExch(&s.key[tile], inf_bits());
+        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
         uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
         s_word[0] = f;
         s_word[1] = 0u;  // abort flag

@@ -57,8 +57,8 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
 
     // Claim and stage.
     if (lane == 0) {
+        uint32_t const kold = atomicExch(&s.key[tile], inf_bits());  // both in flight, as in solve_tile
         uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
-        uint32_t const kold = atomicExch(&s.key[tile], inf_bits());
         uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
         sm.claim[0] = f;
         sm.claim[1] = kold;

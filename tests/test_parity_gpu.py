@@ -197,6 +197,17 @@ def test_bounded_wait_times_out_cleanly(setups):
     assert res.field[1, 1] == 0.0 and np.isfinite(res.field).all()
 
 
+def test_update_sqrt_is_ieee_for_every_float(setups):
+    """The device update's square root (an FMA-corrected hardware estimate)
+    gives the bits of CUDA's IEEE __fsqrt_rn for all 2^32 inputs."""
+    import ctypes
+
+    s = setups(16)
+    bad = ctypes.c_ulonglong(123)
+    assert _lib.load().ghcm_selftest_sqrt(s.handle, ctypes.byref(bad)) == _lib.GHCM_OK
+    assert bad.value == 0
+
+
 def test_device_entry_with_torch_tensors(setups, medium):
     import torch
 
