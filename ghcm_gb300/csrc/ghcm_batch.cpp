@@ -152,7 +152,6 @@ int ghcm_batch_create(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count,
     b->device = ctx->device;
     b->sms = ctx->sms;
     b->launch = ctx->launch;
-    b->grid = ctx->launch.blocks_per_sm * ctx->sms;
     b->count = count;
     b->tiles = static_cast<uint32_t>(tiles);
     b->cells = cells;
@@ -179,6 +178,7 @@ int ghcm_batch_create(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count,
     s.num_tiles = b->tiles;
     s.num_insts = count;
     fill_sched_params(s, b->cfg, b->sms, b->tiles);
+    b->grid = persistent_grid(b->launch, b->sms, s.max_jobs);
     size_t o = 0;
     auto take = [&](size_t bytes) {
         size_t const at = o;

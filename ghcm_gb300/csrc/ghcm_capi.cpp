@@ -161,7 +161,7 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     cudaEventRecord(ctx->ev0, st);
     if ((e = launch_init(s, 1, static_cast<uint64_t>(w) * h, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
         return map_cuda(e);
-    int const grid = ctx->launch.blocks_per_sm * ctx->sms;
+    int const grid = persistent_grid(ctx->launch, ctx->sms, s.max_jobs);
     cudaEventRecord(ctx->ev2, st);
     if ((e = launch_persistent(static_cast<int>(B), ctx->cfg.kernel == GHCM_KERNEL_FIM, s, grid, st)) != cudaSuccess)
         return map_cuda(e);

@@ -63,7 +63,10 @@ struct Ctl {
     unsigned long long prof[24];   // GHCM_PROFILE builds: per-phase nanoseconds and sweep counts
     unsigned long long release_ns; // GHCM_PROFILE builds: when the last barrier was released
     uint32_t wave_max_sweeps;      // GHCM_PROFILE builds: most sweeps of one block-solve in this wave
+    uint32_t sm_far;               // a CTA ran on an SM id >= kMaxSms: jobs go by block index
+    uint32_t sm_ctas[256];         // CTAs of the persistent grid on each SM (by %smid)
 };
+constexpr uint32_t kMaxSms = 256;
 
 // Learned block schedule and trace recorder (see ghcm_learn.cuh).
 constexpr int kFeatures = 12;
@@ -134,7 +137,8 @@ struct Sched {
 // Launch configuration chosen by the host for a (block size, kernel) pair.
 struct LaunchInfo {
     int threads;
-    int blocks_per_sm;
+    int blocks_per_sm;  // most CTAs per SM the grid may use (occupancy, capped)
+    int workers;        // tile workers per CTA: 1, or 8 for one warp per tile
 };
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -149,6 +153,8 @@ bool encode_tile_map(EncodeTiledFn encode, CUtensorMap* map, const float* base, 
 
 // Host entry points implemented in ghcm_solver.cu.
 int query_persistent(int block, int fim, LaunchInfo* info);
+// CTAs of the persistent grid for waves of up to max_jobs tiles.
+int persistent_grid(const LaunchInfo& info, int sms, uint32_t max_jobs);
 // The staged box (elements) of a tile: the TMA tensor maps use it as their box.
 void tile_box(int block, uint32_t* width, uint32_t* height);
 // Initialises the per-tile state, the time fields (+inf, inputs checked) and

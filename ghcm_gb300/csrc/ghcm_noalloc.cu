@@ -33,7 +33,7 @@ namespace ghcm {
 namespace {
 
 constexpr size_t kSlot = static_cast<size_t>(GHCM_NOALLOC_MAX_TILES) * sizeof(uint32_t);
-constexpr size_t kCtlBytes = 512;
+constexpr size_t kCtlBytes = 2048;
 constexpr size_t kInstBytes = 256;
 // flags | key | tmin | list0 | list1 | jobs | control block | instance
 constexpr size_t kScratchBytes = 6 * kSlot + kCtlBytes + kInstBytes;
@@ -138,7 +138,7 @@ extern "C" int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_
     if ((e = cudaMemsetAsync(s.ctl, 0, sizeof(Ctl), st)) != cudaSuccess) return GHCM_ERR_CUDA;
     if ((e = launch_init(s, 1, static_cast<uint64_t>(width) * height, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
         return GHCM_ERR_CUDA;
-    if ((e = launch_persistent(static_cast<int>(B), cfg->kernel == GHCM_KERNEL_FIM, s, li.blocks_per_sm * sms, st)) !=
+    if ((e = launch_persistent(static_cast<int>(B), cfg->kernel == GHCM_KERNEL_FIM, s, persistent_grid(li, sms, s.max_jobs), st)) !=
         cudaSuccess)
         return GHCM_ERR_CUDA;
     uint32_t error = 0u;

@@ -478,6 +478,47 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
     }
 }
 
+// Job order of the persistent grid. Consecutive block indices share SMs
+// (a 608-block launch put blocks 0-15 four to an SM), so a wave with fewer
+// jobs than CTAs would crowd its tiles onto a few SMs. Each CTA instead takes
+// a slot on its SM when it starts (sm_enter) and, once every CTA has entered,
+// ranks itself (sm_rank): first slot 0 of every SM in SM order, then slot 1,
+// and so on - a permutation of 0..gridDim.x-1. Jobs j, j + grid, ... go to
+// rank j.
+__device__ __forceinline__ void sm_enter(Ctl* ctl, uint32_t* s_slot) {
+    uint32_t smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    s_slot[0] = smid;
+    if (smid < kMaxSms)
+        s_slot[1] = atomicAdd(&ctl->sm_ctas[smid], 1u);
+    else
+        atomicOr(&ctl->sm_far, 1u);
+}
+
+// Every thread returns this CTA's rank; call after a grid barrier that
+// follows every CTA's sm_enter.
+template <int THREADS>
+__device__ uint32_t sm_rank(const Ctl* ctl, const uint32_t* s_slot, uint32_t* s_tmp) {
+    static_assert(THREADS >= 32 && THREADS % 32 == 0, "whole warps");
+    int const tid = threadIdx.x;
+    if (ld_relaxed(&ctl->sm_far) != 0u) return blockIdx.x;
+    uint32_t const smid = s_slot[0], slot = s_slot[1];
+    uint32_t part = 0u;
+    for (uint32_t m = tid; m < kMaxSms; m += THREADS) {
+        uint32_t const c = ld_relaxed(&ctl->sm_ctas[m]);
+        part += min(c, slot) + ((m < smid && c > slot) ? 1u : 0u);
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((tid & 31) == 0) s_tmp[tid >> 5] = part;
+    __syncthreads();
+    uint32_t r = 0u;
+#pragma unroll
+    for (int w = 0; w < THREADS / 32; ++w) r += s_tmp[w];
+    __syncthreads();
+    return r;
+}
+
 // Grid-wide wave barrier. Every CTA arrives; the last one to arrive decides
 // the next phase (decide_phase) and releases the others with one 64-bit word
 // that carries the decision, so a released CTA needs no further load. The

@@ -83,6 +83,8 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_
     }
     if (s.learn.params)  // learned schedule: the model in shared memory for scoring
         for (int i = tid; i < kParams; i += G::THREADS) g_mlp_params[i] = __ldg(&s.learn.params[i]);
+    __shared__ uint32_t s_slot[2];
+    if (tid == 0) sm_enter(ctl, s_slot);
     __syncthreads();
     GHCM_PROF_BEGIN(t_kernel);
     uint32_t parity = 0u;
@@ -91,11 +93,17 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_
     uint32_t const warps_per_cta = G::THREADS / 32;
     uint32_t const gw = blockIdx.x * warps_per_cta + static_cast<uint32_t>(tid >> 5);
     uint32_t const nwarps = gridDim.x * warps_per_cta;
+    uint32_t rank = blockIdx.x;
+    bool ranked = false;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
         bool const ok = wave_barrier<G::THREADS, select_cache<B, FIM>()>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
+        if (!ranked) {  // the first barrier follows every CTA's sm_enter
+            rank = sm_rank<G::THREADS>(ctl, s_slot, reinterpret_cast<uint32_t*>(s_red));
+            ranked = true;
+        }
         uint32_t const phase = s_state[kStPhase];
         uint32_t const cur = s_state[kStCur];
         if (phase == kPhaseJobs) {
@@ -104,12 +112,12 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_
             uint32_t const wave = s_state[kStWaves];
             const uint32_t* jobs = s_state[kStInList] ? s.list[cur] : s.jobs;
 #ifdef GHCM_PROFILE
-            if (tid == 0 && blockIdx.x < nj) {  // the latest first-job start of the wave
+            if (tid == 0 && rank < nj) {  // the latest first-job start of the wave
                 unsigned long long const rel = ld_relaxed_u64(&ctl->release_ns);
                 atomicMax(&ctl->prof[16], static_cast<unsigned long long>(global_ns() - rel));
             }
 #endif
-            for (uint32_t j = blockIdx.x; j < nj; j += gridDim.x) {
+            for (uint32_t j = rank; j < nj; j += gridDim.x) {
                 uint32_t const job = __ldcg(&jobs[j]);
                 if (job >= s.num_tiles) {  // never written by a correct decision: stop the grid
                     if (tid == 0) atomicOr(&ctl->error, kErrInternal);
@@ -121,7 +129,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_
                 solves += (r == kJobSolved) ? 1u : 0u;
             }
 #ifdef GHCM_PROFILE
-            if (tid == 0 && blockIdx.x < nj) {  // the latest job end of the wave
+            if (tid == 0 && rank < nj) {  // the latest job end of the wave
                 unsigned long long const rel = ld_relaxed_u64(&ctl->release_ns);
                 atomicMax(&ctl->prof[14], static_cast<unsigned long long>(global_ns() - rel));
             }
@@ -168,6 +176,9 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
     }
     if (s.learn.params)
         for (int i = tid; i < kParams; i += W::THREADS) g_mlp_params[i] = __ldg(&s.learn.params[i]);
+    __shared__ uint32_t s_slot[2];
+    __shared__ uint32_t s_tmp[W::NW];
+    if (tid == 0) sm_enter(ctl, s_slot);
     __syncthreads();
     GHCM_PROF_BEGIN(t_kernel);
     uint32_t parity = 0u;
@@ -175,11 +186,17 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
     unsigned long long solves = 0ull;
     uint32_t const gw = blockIdx.x * W::NW + static_cast<uint32_t>(warp);
     uint32_t const nwarps = gridDim.x * W::NW;
+    uint32_t worker = gw;  // job order: warp 0 of every CTA (by SM rank) first, then warp 1, ...
+    bool ranked = false;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
         bool const ok = wave_barrier<W::THREADS, 4>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
+        if (!ranked) {
+            worker = static_cast<uint32_t>(warp) * gridDim.x + sm_rank<W::THREADS>(ctl, s_slot, s_tmp);
+            ranked = true;
+        }
         uint32_t const phase = s_state[kStPhase];
         uint32_t const cur = s_state[kStCur];
         if (phase == kPhaseJobs) {
@@ -187,7 +204,7 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
             uint32_t const nj = s_state[kStJobs];
             uint32_t const wave = s_state[kStWaves];
             const uint32_t* jobs = s_state[kStInList] ? s.list[cur] : s.jobs;
-            for (uint32_t j = gw; j < nj; j += nwarps) {
+            for (uint32_t j = worker; j < nj; j += nwarps) {
                 uint32_t const job = __ldcg(&jobs[j]);
                 if (job >= s.num_tiles) {
                     if (lane == 0) atomicOr(&ctl->error, kErrInternal);
@@ -363,7 +380,20 @@ int query_persistent(int block, int fim, LaunchInfo* info) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, threads, 0) != cudaSuccess) return -3;
     info->threads = threads;
     info->blocks_per_sm = std::min(bps, cap_for(block, fim));
+    info->workers = warp_tiles(block, fim) ? WarpTileGeom<8>::NW : 1;
     return 0;
+}
+
+// Enough CTAs per SM that every job of a full wave has a worker of its own,
+// within the occupancy cap. Fewer CTAs make the per-wave grid barrier cheaper
+// and crowd an SM's tile solves less: on the 4096^2 seven-ring field with
+// n = 256, 2 CTAs per SM solved in 13.7 ms against 15.6 ms with 4, while
+// n = 1024, the noise field and batches want all 4.
+int persistent_grid(const LaunchInfo& info, int sms, uint32_t max_jobs) {
+    uint64_t const per_round = static_cast<uint64_t>(std::max(1, info.workers)) * static_cast<uint64_t>(sms);
+    uint64_t const want = (static_cast<uint64_t>(max_jobs) + per_round - 1u) / per_round;
+    int const per_sm = static_cast<int>(std::min<uint64_t>(std::max(1, info.blocks_per_sm), std::max<uint64_t>(1u, want)));
+    return per_sm * sms;
 }
 
 cudaError_t launch_init(const Sched& s, uint32_t n_insts, uint64_t max_cells, uint32_t max_seeds, int block,
