@@ -102,6 +102,10 @@ inline void print_profile(const Ctl& c, int grid) {
         std::fprintf(stderr, "[ghcm-prof] per wave, after the release: latest first-job start %.2f us, latest job end "
                      "%.2f us, longest block-solve %.2f us\n",
                      c.prof[17] / 1e3 / c.prof[9], c.prof[15] / 1e3 / c.prof[9], c.prof[19] / 1e3 / c.prof[9]);
+    if (c.prof[9])
+        std::fprintf(stderr, "[ghcm-prof] per wave, decision: control loads %.2f us, job planning %.2f us; "
+                     "%.0f%% of waves ran the top-n select\n",
+                     c.prof[20] / 1e3 / c.prof[9], c.prof[21] / 1e3 / c.prof[9], 100.0 * c.prof[22] / c.prof[9]);
     if (c.prof[13])
         std::fprintf(stderr, "[ghcm-prof] per CTA block-solve: stage %.2f us, sweeps %.2f us (%.3f us/sweep), "
                      "probe+commit+activate %.2f us\n",

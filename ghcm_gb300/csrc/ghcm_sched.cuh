@@ -427,6 +427,9 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
     uint32_t phase = kPhaseJobs, ncur = cur;
     {
         uint32_t const act = (prev == kPhaseInit) ? 0u : (cur ^ 1u);
+#ifdef GHCM_PROFILE
+        if (tid == 0) ctl->prof[23] = global_ns();  // decision start
+#endif
         // every control word the decision reads, in one round trip
         uint32_t const m = ld_relaxed(&ctl->count[act]);
         uint32_t const klo = ld_relaxed(&ctl->krange[act][0]);
@@ -465,11 +468,21 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
                 atomicMax(&ctl->max_active, m);
             }
             ncur = act;
+#ifdef GHCM_PROFILE
+            uint64_t const p_sel0 = global_ns();
+#endif
             if (s.learn.params && !s.learn.veto)
                 ncur = plan_learned_jobs<THREADS, CACHE>(s, act, m, lo, hi, s_hist, s_sel);
             else
                 plan_plain_jobs<THREADS, CACHE>(s, act, m, s.max_jobs, 0u, lo, hi, s_hist, s_sel);
             if (tid == 0) atomicAdd(&ctl->waves, 1u);
+#ifdef GHCM_PROFILE
+            if (tid == 0) {  // [20] decision loads, [21] job planning, [22] waves that ran the top-n select
+                ctl->prof[20] += p_sel0 - ctl->prof[23];
+                ctl->prof[21] += global_ns() - p_sel0;
+                if (m > s.max_jobs) ctl->prof[22] += 1u;
+            }
+#endif
         }
     }
     if (tid == 0) {
