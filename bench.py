@@ -163,13 +163,20 @@ def _cpu_name() -> str:
     return os.uname().machine
 
 
-def load_traffic():
-    p = ROOT / "profiles" / "k_solve_ring7_4096.json"
+def load_traffic(name: str = "k_solve_ring7_4096.json", block: int | None = None, n: int | None = None):
+    """DRAM bytes per launch from a committed ncu summary (profiles/), or None;
+    with block / n given, only when the capture used that tile size and n."""
+    p = ROOT / "profiles" / name
     if p.exists():
         try:
-            return json.loads(p.read_text()).get("dram_bytes_per_launch")
+            d = json.loads(p.read_text())
         except (ValueError, OSError):
             return None
+        if block is not None and d.get("block") not in (None, block):
+            return None
+        if n is not None and d.get("n") not in (None, n):
+            return None
+        return d.get("dram_bytes_per_launch")
     return None
 
 
@@ -380,7 +387,10 @@ def run_batched(args, world, rank, local) -> int:
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
     t0 = time.perf_counter()
-    best, trials = g.autotune_batch(g.HcmConfig(block_size=16, fim_minimum_change=EPS), dinst, reps=1)
+    if args.no_autotune:  # a fixed tile size and n (e.g. for a profiler capture of the timed launch)
+        best, trials = g.HcmConfig(block_size=args.block, max_jobs=args.n, fim_minimum_change=EPS), []
+    else:
+        best, trials = g.autotune_batch(g.HcmConfig(block_size=16, fim_minimum_change=EPS), dinst, reps=1)
     tune_s = time.perf_counter() - t0
     setup = g.HcmSetup(best)
     batch = g.Batch(setup, dinst)
@@ -448,7 +458,8 @@ def run_batched(args, world, rank, local) -> int:
                 "h2d_bytes_per_step": sum(4 * i.speed.size for i in insts),
                 "d2h_bytes_per_step": sum(4 * i.speed.size for i in insts)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": f"k_solve<{B},systolic> (batch)",
+                     "traffic": load_traffic("k_solve_batch512.json", B, info["max_jobs"]),
+                     "kernel": f"k_solve<{B},systolic> (batch)",
                      "bytes_per_block_solve": bytes_per_solve(B), "block_solves": solves,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in peaks else "fallback"},
         "autotune": trials,
@@ -601,6 +612,8 @@ def main() -> int:
     ap.add_argument("--no-n-sweep", action="store_true", help="time only the headline n")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain comparison")
     ap.add_argument("--workload", default="ring", choices=["ring", "batched", "maze"])
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batched workload: use --block and --n instead of the autotuner's choice")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
