@@ -379,11 +379,23 @@ def run_batched(args, world, rank, local) -> int:
     insts = [all_insts[i] for i in mine]
     cells = sum(i.speed.size for i in insts)
     total_cells = sum(i.speed.size for i in all_insts)
-    h_speed = [torch.from_numpy(i.speed).pin_memory() for i in insts]
-    h_time = [torch.empty(i.speed.shape, dtype=torch.float32).pin_memory() for i in insts]
-    dinst = [g.DeviceInstance(hs.to(dev), torch.from_numpy(i.seeds.astype(np.int32)).to(dev),
-                              torch.empty(i.speed.shape, dtype=torch.float32, device=dev))
-             for hs, i in zip(h_speed, insts)]
+    # every instance's speed and time field packed in one buffer each (host
+    # pinned and device), at 256-byte aligned offsets, so the end-to-end step
+    # moves the batch with one copy each way
+    offs, at = [], 0
+    for i in insts:
+        offs.append(at)
+        at += (i.speed.size + 63) // 64 * 64
+    h_speed_all = torch.empty(at, dtype=torch.float32).pin_memory()
+    h_time_all = torch.empty(at, dtype=torch.float32).pin_memory()
+    d_speed_all = torch.empty(at, dtype=torch.float32, device=dev)
+    d_time_all = torch.empty(at, dtype=torch.float32, device=dev)
+    view = lambda buf, k: buf[offs[k]:offs[k] + insts[k].speed.size].view(insts[k].speed.shape)
+    for k, i in enumerate(insts):
+        view(h_speed_all, k).copy_(torch.from_numpy(i.speed))
+    d_speed_all.copy_(h_speed_all)
+    dinst = [g.DeviceInstance(view(d_speed_all, k), torch.from_numpy(i.seeds.astype(np.int32)).to(dev),
+                              view(d_time_all, k)) for k, i in enumerate(insts)]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
     t0 = time.perf_counter()
@@ -426,11 +438,9 @@ def run_batched(args, world, rank, local) -> int:
     for _ in range(max(1, min(args.steps, 3))):
         barrier()
         t0 = time.perf_counter()
-        for hs, di in zip(h_speed, dinst):
-            di.d_field.copy_(hs, non_blocking=True)
+        d_speed_all.copy_(h_speed_all, non_blocking=True)
         batch.run(stream)
-        for ht, di in zip(h_time, dinst):
-            ht.copy_(di.d_time, non_blocking=True)
+        h_time_all.copy_(d_time_all, non_blocking=True)
         torch.cuda.synchronize(dev)
         e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = sum(e2e) / len(e2e)
@@ -455,8 +465,8 @@ def run_batched(args, world, rank, local) -> int:
                    "l2": "flushed between steps (256 MiB write outside the events)",
                    "parallelism": f"instances split over {world} rank(s)"},
         "e2e": {"value": total_cells / (e2e_ms * 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": sum(4 * i.speed.size for i in insts),
-                "d2h_bytes_per_step": sum(4 * i.speed.size for i in insts)},
+                "h2d_bytes_per_step": 4 * at, "d2h_bytes_per_step": 4 * at,
+                "layout": "all instances in one pinned buffer each way (256-byte aligned offsets), one copy each"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": load_traffic("k_solve_batch512.json", B, info["max_jobs"]),
                      "kernel": f"k_solve<{B},systolic> (batch)",
