@@ -64,7 +64,7 @@ cudaError_t enqueue(ghcm_batch* b, cudaStream_t st) {
         cudaSuccess)
         return e;
     if ((e = launch_persistent(static_cast<int>(b->cfg.block_size), b->cfg.kernel == GHCM_KERNEL_FIM, b->s, b->grid,
-                               st)) != cudaSuccess)
+                               st, b->launch.wide)) != cudaSuccess)
         return e;
     return cudaMemcpyAsync(b->h_ctl, b->s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
 }
@@ -151,7 +151,10 @@ int ghcm_batch_create(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count,
     b->cfg = ctx->cfg;
     b->device = ctx->device;
     b->sms = ctx->sms;
-    b->launch = ctx->launch;
+    if (query_persistent(static_cast<int>(ctx->cfg.block_size), ctx->cfg.kernel == GHCM_KERNEL_FIM, &b->launch, true) !=
+            0 ||
+        b->launch.blocks_per_sm <= 0)
+        b->launch = ctx->launch;
     b->count = count;
     b->tiles = static_cast<uint32_t>(tiles);
     b->cells = cells;

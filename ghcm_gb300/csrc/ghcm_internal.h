@@ -139,6 +139,7 @@ struct LaunchInfo {
     int threads;
     int blocks_per_sm;  // most CTAs per SM the grid may use (occupancy, capped)
     int workers;        // tile workers per CTA: 1, or 8 for one warp per tile
+    bool wide;          // the 8-CTA-per-SM build of k_solve<16, systolic> (batches)
 };
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -152,7 +153,8 @@ bool encode_tile_map(EncodeTiledFn encode, CUtensorMap* map, const float* base, 
                      uint32_t block);
 
 // Host entry points implemented in ghcm_solver.cu.
-int query_persistent(int block, int fim, LaunchInfo* info);
+// wide: the build for batches with more CTAs per SM, where there is one.
+int query_persistent(int block, int fim, LaunchInfo* info, bool wide = false);
 // CTAs of the persistent grid for waves of up to max_jobs tiles.
 int persistent_grid(const LaunchInfo& info, int sms, uint32_t max_jobs);
 // The staged box (elements) of a tile: the TMA tensor maps use it as their box.
@@ -161,7 +163,7 @@ void tile_box(int block, uint32_t* width, uint32_t* height);
 // the seeds of every instance. max_cells / max_seeds: the largest instance.
 cudaError_t launch_init(const Sched& s, uint32_t n_insts, uint64_t max_cells, uint32_t max_seeds, int block,
                         cudaStream_t st);
-cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cudaStream_t st);
+cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cudaStream_t st, bool wide = false);
 cudaError_t launch_wait_selftest(uint32_t* flag, Ctl* ctl, uint64_t timeout_ns, cudaStream_t st);
 // Every 32-bit float through the solver's square root and __fsqrt_rn; adds the
 // number of differing results to *mismatches (device memory).

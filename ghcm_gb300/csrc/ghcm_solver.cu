@@ -51,6 +51,13 @@ constexpr int max_ctas_per_sm() {
     return B == 8 ? 12 : 4;
 }
 
+// Batches of B=16 systolic tiles use a build for 8 CTAs per SM (32 registers a
+// thread, a few spills outside the sweep loop): their waves hold thousands of
+// jobs, and the extra tiles in flight per SM took a 512-instance batch from
+// 29.5 to 27.4 ms. Single fields keep 4 per SM, where the wider build's
+// register budget slowed the sweeps (rings 13.8 -> 14.4 ms).
+constexpr int kWideCtas = 8;
+
 // Keys per thread the top-n select keeps in registers between its passes: as
 // many as fit in the kernel's register budget without spills.
 template <int B, bool FIM>
@@ -58,8 +65,8 @@ __host__ __device__ constexpr int select_cache() {
     return B == 32 ? (FIM ? 1 : 2) : 4;
 }
 
-template <int B, bool FIM>
-__global__ void __launch_bounds__(TileGeom<B>::THREADS, max_ctas_per_sm<B>()) k_solve(const __grid_constant__ Sched s) {
+template <int B, bool FIM, int CTAS = max_ctas_per_sm<B>()>
+__global__ void __launch_bounds__(TileGeom<B>::THREADS, CTAS) k_solve(const __grid_constant__ Sched s) {
     using G = TileGeom<B>;
     __shared__ TileSmem<B> sm;
     __shared__ __align__(8) uint64_t s_bar;
@@ -335,7 +342,8 @@ static void* kernel_ptr() {
 // shorter spread over 8 warps).
 static bool warp_tiles(int block, int fim) { return !fim && block == 8; }
 
-static void* select_kernel(int block, int fim) {
+static void* select_kernel(int block, int fim, bool wide) {
+    if (wide && block == 16 && !fim) return reinterpret_cast<void*>(&k_solve<16, false, kWideCtas>);
     switch (block) {
         case 8: return fim ? kernel_ptr<8, true>() : reinterpret_cast<void*>(&k_solve_warp<8>);
         case 16: return fim ? kernel_ptr<16, true>() : kernel_ptr<16, false>();
@@ -354,8 +362,9 @@ static int threads_for(int block, int fim) {
     }
 }
 
-static int cap_for(int block, int fim) {
+static int cap_for(int block, int fim, bool wide) {
     if (warp_tiles(block, fim)) return 4;
+    if (wide && block == 16 && !fim) return kWideCtas;
     switch (block) {
         case 8: return max_ctas_per_sm<8>();
         case 16: return max_ctas_per_sm<16>();
@@ -372,14 +381,15 @@ void tile_box(int block, uint32_t* width, uint32_t* height) {
     }
 }
 
-int query_persistent(int block, int fim, LaunchInfo* info) {
-    void* k = select_kernel(block, fim);
+int query_persistent(int block, int fim, LaunchInfo* info, bool wide) {
+    void* k = select_kernel(block, fim, wide);
     if (!k) return -1;
     int const threads = threads_for(block, fim);
     int bps = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, threads, 0) != cudaSuccess) return -3;
     info->threads = threads;
-    info->blocks_per_sm = std::min(bps, cap_for(block, fim));
+    info->blocks_per_sm = std::min(bps, cap_for(block, fim, wide));
+    info->wide = wide && block == 16 && !fim;
     info->workers = warp_tiles(block, fim) ? WarpTileGeom<8>::NW : 1;
     return 0;
 }
@@ -421,8 +431,8 @@ cudaError_t launch_init(const Sched& s, uint32_t n_insts, uint64_t max_cells, ui
     return cudaGetLastError();
 }
 
-cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cudaStream_t st) {
-    void* k = select_kernel(block, fim);
+cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cudaStream_t st, bool wide) {
+    void* k = select_kernel(block, fim, wide);
     if (!k) return cudaErrorInvalidValue;
     void* args[] = {const_cast<Sched*>(&s)};
     // A learned-schedule launch stages the model in dynamic shared memory; its
