@@ -317,7 +317,22 @@ def small_ring_check(g) -> dict:
             "waves": res.stats["waves"], "device_ms": res.stats["device_ms"], "cpu_fim_ms": us_fim / 1e3,
             "cpu_fmm_ms": us_fmm / 1e3, "max_rel_vs_fim": rel_diff(res.field, fim),
             "max_rel_vs_fmm": rel_diff(res.field, fmm), "vs_fmm64": fmm64_errors(res.field, ref64),
-            "fim_vs_fmm64": fmm64_errors(fim, ref64)}
+            "fim_vs_fmm64": fmm64_errors(fim, ref64),
+            "reference_schedule": reference_schedule(o, cost, seeds, 8, 64, 64, fim)}
+
+
+def reference_schedule(o, cost, seeds, block: int, n: int, wg: int, fim) -> dict:
+    """The reference's own gHCM schedule on the same field, restated on the CPU
+    by the oracle (stale priority keys, the dirty set cleared after the wave so
+    a block dirtied in flight is lost, check_border writing into neighbours,
+    no residual check; one work-group of wg lanes per tile): its block-solves
+    and waves, and how far its field ends from the fixed point."""
+    from oracle.oracle import rel_diff
+
+    out, solves, waves = o.hcm(cost, seeds, block=block, max_jobs=n, eps=EPS, wg=wg)
+    return {"block": block, "n": n, "work_group": wg, "block_solves": int(solves), "waves": int(waves),
+            "max_rel_vs_fim": rel_diff(out, fim), "residual": o.residual(cost, out),
+            "note": "CPU restatement; the wave's jobs run one after another"}
 
 
 def learned_vs_plain(g, dev, stream, flush, steps: int, warmup: int, fp64: bool = True) -> dict:
@@ -363,13 +378,23 @@ def learned_vs_plain(g, dev, stream, flush, steps: int, warmup: int, fp64: bool 
 
         build(with_reference=False)
         ref64, _ = Oracle().fmm64(fields.cost_from_speed(speed), seeds)
+    ref_sched = None
+    if fp64:  # the reference's own schedule, restated on the CPU (checker only)
+        o = Oracle()
+        cost = fields.cost_from_speed(speed)
+        ref_sched = reference_schedule(o, cost, seeds, 16, 1024, 256, o.fim(cost, seeds, EPS)[0])
     for name in runs:
         out[name]["solves_vs_plain_n1024"] = out[name]["block_solves"] / base
         out[name]["max_rel_vs_plain_n1024"] = rel_diff(fields_out[name], fields_out["plain_n1024"])
         if ref64 is not None:
             out[name]["vs_fmm64"] = fmm64_errors(fields_out[name], ref64)
-    return {"workload": "noise_4096x4096_16src", "seed": NOISE_EVAL_SEED, "threshold": threshold,
-            "model": MODEL.name, "train_seeds": int(len(meta.get("train_seeds", []))), "runs": out}
+        if ref_sched is not None:
+            out[name]["solves_vs_reference_schedule"] = out[name]["block_solves"] / ref_sched["block_solves"]
+    res = {"workload": "noise_4096x4096_16src", "seed": NOISE_EVAL_SEED, "threshold": threshold,
+           "model": MODEL.name, "train_seeds": int(len(meta.get("train_seeds", []))), "runs": out}
+    if ref_sched is not None:
+        res["reference_schedule_n1024"] = ref_sched
+    return res
 
 
 def run_batched(args, world, rank, local) -> int:
