@@ -475,7 +475,7 @@ def run_batched(args, world, rank, local) -> int:
 
     # end to end: pinned host fields in, every time field out, inside the timed region
     e2e = []
-    for it in range(1 + max(1, min(args.steps, 3))):  # the first pass is an untimed warm-up
+    for it in range(1 + max(3, min(args.steps, 5))):  # the first pass is an untimed warm-up
         barrier()
         t0 = time.perf_counter()
         d_speed_all.copy_(h_speed_all, non_blocking=True)

@@ -161,9 +161,13 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     cudaEventRecord(ctx->ev0, st);
     if ((e = launch_init(s, 1, static_cast<uint64_t>(w) * h, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
         return map_cuda(e);
-    int const grid = persistent_grid(ctx->launch, ctx->sms, s.max_jobs);
+    // the wide build for plain waves of many jobs; the learned schedule keeps the
+    // register budget its scoring was measured with
+    bool const wide = !learned && wide_for(ctx->launch, ctx->sms, s.max_jobs) && ctx->wide.blocks_per_sm > 0;
+    LaunchInfo const& li = wide ? ctx->wide : ctx->launch;
+    int const grid = persistent_grid(li, ctx->sms, s.max_jobs);
     cudaEventRecord(ctx->ev2, st);
-    if ((e = launch_persistent(static_cast<int>(B), ctx->cfg.kernel == GHCM_KERNEL_FIM, s, grid, st)) != cudaSuccess)
+    if ((e = launch_persistent(static_cast<int>(B), ctx->cfg.kernel == GHCM_KERNEL_FIM, s, grid, st, li.wide)) != cudaSuccess)
         return map_cuda(e);
     cudaEventRecord(ctx->ev1, st);
     if ((e = cudaMemcpyAsync(ctx->h_ctl, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
@@ -266,6 +270,8 @@ int ghcm_create(const ghcm_config* cfg, ghcm_ctx** out) {
     ctx->cfg = *cfg;
     ctx->device = dev;
     ctx->sms = sms;
+    if (query_persistent(static_cast<int>(cfg->block_size), cfg->kernel == GHCM_KERNEL_FIM, &ctx->wide, true) != 0)
+        ctx->wide.blocks_per_sm = 0;  // no wide build: every solve uses ctx->launch
     if (query_persistent(static_cast<int>(cfg->block_size), cfg->kernel == GHCM_KERNEL_FIM, &ctx->launch) != 0 ||
         ctx->launch.blocks_per_sm <= 0) {
         delete ctx;

@@ -137,6 +137,7 @@ struct ghcm_ctx {
     int device = 0;
     int sms = 0;
     ghcm::LaunchInfo launch{};
+    ghcm::LaunchInfo wide{};    // the build with more CTAs per SM for waves of many jobs (blocks_per_sm 0: none)
     ghcm::EncodeTiledFn encode = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
     // scheduler workspace: flags | key | tmin | list0 | list1 | jobs | ctl | insts

@@ -139,7 +139,7 @@ struct LaunchInfo {
     int threads;
     int blocks_per_sm;  // most CTAs per SM the grid may use (occupancy, capped)
     int workers;        // tile workers per CTA: 1, or 8 for one warp per tile
-    bool wide;          // the 8-CTA-per-SM build of k_solve<16, systolic> (batches)
+    bool wide;          // the 8-CTA-per-SM build of k_solve<16 or 32, systolic>
 };
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -157,6 +157,9 @@ bool encode_tile_map(EncodeTiledFn encode, CUtensorMap* map, const float* base, 
 int query_persistent(int block, int fim, LaunchInfo* info, bool wide = false);
 // CTAs of the persistent grid for waves of up to max_jobs tiles.
 int persistent_grid(const LaunchInfo& info, int sms, uint32_t max_jobs);
+// Whether a single field with waves of up to max_jobs tiles runs the wide
+// build (more CTAs per SM) rather than `narrow`.
+bool wide_for(const LaunchInfo& narrow, int sms, uint32_t max_jobs);
 // The staged box (elements) of a tile: the TMA tensor maps use it as their box.
 void tile_box(int block, uint32_t* width, uint32_t* height);
 // Initialises the per-tile state, the time fields (+inf, inputs checked) and

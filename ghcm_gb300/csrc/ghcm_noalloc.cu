@@ -138,7 +138,12 @@ extern "C" int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_
     if ((e = cudaMemsetAsync(s.ctl, 0, sizeof(Ctl), st)) != cudaSuccess) return GHCM_ERR_CUDA;
     if ((e = launch_init(s, 1, static_cast<uint64_t>(width) * height, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
         return GHCM_ERR_CUDA;
-    if ((e = launch_persistent(static_cast<int>(B), cfg->kernel == GHCM_KERNEL_FIM, s, persistent_grid(li, sms, s.max_jobs), st)) !=
+    LaunchInfo wl{};
+    if (wide_for(li, sms, s.max_jobs) &&
+        query_persistent(static_cast<int>(B), cfg->kernel == GHCM_KERNEL_FIM, &wl, true) == 0 && wl.blocks_per_sm > 0)
+        li = wl;
+    if ((e = launch_persistent(static_cast<int>(B), cfg->kernel == GHCM_KERNEL_FIM, s, persistent_grid(li, sms, s.max_jobs), st,
+                               li.wide)) !=
         cudaSuccess)
         return GHCM_ERR_CUDA;
     uint32_t error = 0u;

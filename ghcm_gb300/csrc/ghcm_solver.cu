@@ -51,11 +51,15 @@ constexpr int max_ctas_per_sm() {
     return B == 8 ? 12 : 4;
 }
 
-// Batches of B=16 systolic tiles use a build for 8 CTAs per SM (32 registers a
-// thread, a few spills outside the sweep loop): their waves hold thousands of
-// jobs, and the extra tiles in flight per SM took a 512-instance batch from
-// 29.5 to 27.4 ms. Single fields keep 4 per SM, where the wider build's
-// register budget slowed the sweeps (rings 13.8 -> 14.4 ms).
+// Systolic B=16 and B=32 tiles also have a build for 8 CTAs per SM (32
+// registers a thread, a few spills outside the sweep loop) for waves that hold
+// many jobs per CTA: batches, and single fields whose n is more than twice the
+// 4-CTA grid (wide_for). The extra tiles in flight per SM took a 512-instance
+// batch from 29.5 to 27.4 ms at B=16 and from 32.1 to 28.2 ms at B=32, the
+// 16384^2 maze (B=32, n=4096) from 98.5 to 95.5 ms and the 4096^2 rings at
+// n=4096 from 19.7 to 19.0 ms. With fewer jobs per CTA the smaller register
+// budget costs more than the extra tiles bring (rings at n=256: 13.8 -> 14.4
+// ms, at n=1024: 16.2 -> 16.5 ms), so those keep the 4-CTA build.
 constexpr int kWideCtas = 8;
 
 // Keys per thread the top-n select keeps in registers between its passes: as
@@ -344,6 +348,7 @@ static bool warp_tiles(int block, int fim) { return !fim && block == 8; }
 
 static void* select_kernel(int block, int fim, bool wide) {
     if (wide && block == 16 && !fim) return reinterpret_cast<void*>(&k_solve<16, false, kWideCtas>);
+    if (wide && block == 32 && !fim) return reinterpret_cast<void*>(&k_solve<32, false, kWideCtas>);
     switch (block) {
         case 8: return fim ? kernel_ptr<8, true>() : reinterpret_cast<void*>(&k_solve_warp<8>);
         case 16: return fim ? kernel_ptr<16, true>() : kernel_ptr<16, false>();
@@ -364,7 +369,7 @@ static int threads_for(int block, int fim) {
 
 static int cap_for(int block, int fim, bool wide) {
     if (warp_tiles(block, fim)) return 4;
-    if (wide && block == 16 && !fim) return kWideCtas;
+    if (wide && (block == 16 || block == 32) && !fim) return kWideCtas;
     switch (block) {
         case 8: return max_ctas_per_sm<8>();
         case 16: return max_ctas_per_sm<16>();
@@ -389,7 +394,7 @@ int query_persistent(int block, int fim, LaunchInfo* info, bool wide) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, threads, 0) != cudaSuccess) return -3;
     info->threads = threads;
     info->blocks_per_sm = std::min(bps, cap_for(block, fim, wide));
-    info->wide = wide && block == 16 && !fim;
+    info->wide = wide && (block == 16 || block == 32) && !fim;
     info->workers = warp_tiles(block, fim) ? WarpTileGeom<8>::NW : 1;
     return 0;
 }
@@ -399,6 +404,11 @@ int query_persistent(int block, int fim, LaunchInfo* info, bool wide) {
 // and crowd an SM's tile solves less: on the 4096^2 seven-ring field with
 // n = 256, 2 CTAs per SM solved in 13.7 ms against 15.6 ms with 4, while
 // n = 1024, the noise field and batches want all 4.
+bool wide_for(const LaunchInfo& narrow, int sms, uint32_t max_jobs) {
+    return static_cast<uint64_t>(max_jobs) >
+           2u * static_cast<uint64_t>(std::max(1, narrow.blocks_per_sm)) * static_cast<uint64_t>(std::max(1, sms));
+}
+
 int persistent_grid(const LaunchInfo& info, int sms, uint32_t max_jobs) {
     uint64_t const per_round = static_cast<uint64_t>(std::max(1, info.workers)) * static_cast<uint64_t>(sms);
     uint64_t const want = (static_cast<uint64_t>(max_jobs) + per_round - 1u) / per_round;
