@@ -102,6 +102,9 @@ class Clocks:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            # let the sampler finish starting up (NVML initialisation) before the
+            # timed region: a step overlapping it once measured 150 ms longer
+            time.sleep(0.5)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -726,6 +729,7 @@ def main() -> int:
     clocks = clk.summary()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     kernel_ms = [st["kernel_ms"] for st in stats]
+    step_spread = {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}
     ms = sum(step_ms) / len(step_ms)
     if dist is not None:
         t = torch.tensor([ms], device=dev)
@@ -787,8 +791,8 @@ def main() -> int:
     peak = peaks.get("hbm_gbs", 6800.0)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "warmup": args.warmup, "ms_per_step": ms, "step_ms": step_spread, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "block": args.block, "n": args.n, "kernel": args.kernel, "eps": EPS,
                    "sources": int(len(seeds)), "l2": "flushed between steps (256 MiB write outside the events)",
                    "parallelism": f"replicas x{world}"},
