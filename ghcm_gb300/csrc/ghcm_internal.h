@@ -23,7 +23,7 @@ enum : uint32_t {
 // Per-tile scheduler flags.
 enum : uint32_t {
     kActive   = 1u << 0,   // tile is in the active set (queued or about to be)
-    kFull     = 1u << 1,   // re-solve every cell (residual judge, sweep cap)
+    kFull     = 1u << 1,   // re-solve every cell (residual check, sweep cap)
     kEdgeBit0 = 1u << 4,   // edge e of the tile received new boundary values: kEdgeBit0 << e
     kEdgeMask = 0xFu << 4,
 };

@@ -5,9 +5,9 @@
 // (src/eikonal_hcm.cpp:47-80, 344-358). The learned schedule scores every
 // active tile with a 12 -> 64 -> 64 -> 1 FP32 MLP (the CTA that queues a tile
 // scores it right after its own solve) and solves those scoring at or above a
-// threshold (tiles re-queued by the residual judge or a sweep cap always go),
+// threshold (tiles re-queued by the residual check or a sweep cap always go),
 // filled up to fallback_jobs in the plain key order. The global Godunov
-// residual judge is unchanged, so a wrong score costs work, never accuracy.
+// residual check is unchanged, so a wrong score costs work, never accuracy.
 //
 // The same features are written, with the outcome of each solve, by the
 // trace recorder of the plain solver; the model is trained on those traces
@@ -27,7 +27,7 @@ namespace ghcm {
 //   7 active neighbours / 4
 //   8 waves since the tile's last useful solve / 64 (1: never)
 //   9 log2(1 + solves so far) / 8
-//  10 re-queued in full (residual judge or sweep cap)
+//  10 re-queued in full (residual check or sweep cap)
 //  11 edges with new boundary values / 4
 // key/kmax: the tile's activation keys (float), flags: its scheduler flags.
 __device__ __forceinline__ void tile_features(const Sched& s, uint32_t tile, uint32_t flags, float key, float kmax,

@@ -15,7 +15,7 @@
 //              (src/eikonal_hcm.cpp:434-469);
 //   when no tile is active, a global Godunov residual pass over every cell
 //   re-activates any tile not at the fixed point; the solve ends when that
-//   pass activates nothing. The reference has no such judge
+//   pass activates nothing. The reference has no such check
 //   (src/eikonal_hcm.cpp:343, 486-488).
 //
 // Every wait (grid barrier, TMA completion) is bounded by Sched::timeout_ns.

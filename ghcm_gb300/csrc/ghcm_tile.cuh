@@ -15,7 +15,7 @@
 //             than eps opens (data/eikonal_ghcm_fim.cl:166-210, 347-372).
 //             The initial open set is the rows of the edges neighbours
 //             flagged (fim.cl:306-332), the cells next to seeds and, for tiles
-//             re-queued by the residual judge, every cell.
+//             re-queued by the residual check, every cell.
 //
 // Then each neighbour edge row is probed with the converged tile
 // (check_border, data/eikonal_ghcm_systolic.cl:8-41) - probe-only, as
@@ -389,7 +389,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     return kJobSolved;
 }
 
-// Global residual judge, one tile per warp: re-activates every tile holding
+// Global residual check, one tile per warp: re-activates every tile holding
 // a cell whose Godunov update would still lower it by more than eps. The
 // reference has no such check (src/eikonal_hcm.cpp:343, 486-488).
 template <int B>

@@ -203,7 +203,7 @@ int ghcm_autotune_batch(const ghcm_config* base, const ghcm_instance* insts, uin
  * (ReLU, sigmoid output) scores each active tile with P(its solve moves some
  * cell by more than eps). With cfg.schedule = GHCM_SCHEDULE_LEARNED and a
  * model set, every wave solves the tiles scoring >= threshold (plus tiles
- * re-queued by the residual judge or a sweep cap), up to cfg.max_jobs; a wave
+ * re-queued by the residual check or a sweep cap), up to cfg.max_jobs; a wave
  * in which none qualifies falls back to the plain top-n. The global Godunov
  * residual check still decides convergence.
  *

@@ -20,7 +20,7 @@ from oracle.oracle import rel_diff
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-5  # spec parity bar: max relative difference vs the reference FIM
+TOL = 1e-5  # the parity bar: max relative difference vs the reference FIM
 
 
 @pytest.fixture(scope="module")
