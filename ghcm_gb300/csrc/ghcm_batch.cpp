@@ -249,6 +249,7 @@ int ghcm_batch_run(ghcm_batch* b, void* stream, ghcm_stats* stats) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return map_cuda(e);
     Ctl const& c = *b->h_ctl;
+    report_checks(c);
     print_profile(c, b->grid);
     if (stats) {
         float ms = 0.f;

@@ -181,6 +181,7 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     ctx->counters[1] = c.fallback_waves;
     ctx->counters[2] = c.trace_count;
     ctx->counters[3] = c.vetoes;
+    report_checks(c);
     print_profile(c, grid);
     if (stats) {
         float ms = 0.f, kms = 0.f;

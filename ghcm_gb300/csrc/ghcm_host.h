@@ -73,7 +73,7 @@ inline int status_from_error(uint32_t error) {
     if (error & kErrBadSeed) return GHCM_ERR_BAD_ARG;
     if (error & kErrBadInput) return GHCM_ERR_BAD_INPUT;
     if (error & kErrTimeout) return GHCM_ERR_TIMEOUT;
-    if (error & kErrInternal) return GHCM_ERR_INTERNAL;
+    if (error & (kErrInternal | kErrChecked)) return GHCM_ERR_INTERNAL;
     if (error & kErrNotConverged) return GHCM_ERR_NOT_CONVERGED;
     return GHCM_OK;
 }
@@ -89,6 +89,17 @@ inline float cost_cap_of(const ghcm_config& cfg) {
 }
 
 // GHCM_PROFILE builds: the per-phase counters of a finished solve, on stderr.
+// GHCM_CHECKED builds: names a failed index check on stderr (the solve also
+// returns GHCM_ERR_INTERNAL).
+inline void report_checks(const Ctl& c) {
+#ifdef GHCM_CHECKED
+    if (c.error & kErrChecked)
+        std::fprintf(stderr, "[ghcm-checked] an index check failed; largest failing site id %u\n", c.check_site);
+#else
+    (void)c;
+#endif
+}
+
 inline void print_profile(const Ctl& c, int grid) {
 #ifdef GHCM_PROFILE
     std::fprintf(stderr,

@@ -18,6 +18,7 @@ enum : uint32_t {
     kErrNotConverged = 1u << 2,  // wave cap reached
     kErrInternal     = 1u << 3,  // list overflow or an impossible state
     kErrBadSeed      = 1u << 4,  // a device-resident seed lies outside its field
+    kErrChecked      = 1u << 5,  // GHCM_CHECKED builds: an index check failed (Ctl::check_site)
 };
 
 // Per-tile scheduler flags.
@@ -63,6 +64,7 @@ struct Ctl {
     unsigned long long prof[24];   // GHCM_PROFILE builds: per-phase nanoseconds and sweep counts
     unsigned long long release_ns; // GHCM_PROFILE builds: when the last barrier was released
     uint32_t wave_max_sweeps;      // GHCM_PROFILE builds: most sweeps of one block-solve in this wave
+    uint32_t check_site;           // GHCM_CHECKED builds: largest id of a failed index check
     uint32_t sm_far;               // a CTA ran on an SM id >= kMaxSms: jobs go by block index
     uint32_t sm_ctas[256];         // CTAs of the persistent grid on each SM (by %smid)
 };

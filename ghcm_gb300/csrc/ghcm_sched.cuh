@@ -241,10 +241,13 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
         int const b = bin_of(__uint_as_float(kb));
         bool take = b < bnd;
         if (!take && b == bnd) take = atomicAdd(&s_sel[2], 1u) < take_eq;
-        if (take)
-            s.jobs[jobs_base + atomicAdd(&s_sel[3], 1u)] = t;
-        else
-            carry[atomicAdd(&s_sel[4], 1u)] = t;
+        if (take) {
+            uint32_t const pos = jobs_base + atomicAdd(&s_sel[3], 1u);
+            if (GHCM_CHECK(s.ctl, pos < s.max_jobs, 9u)) s.jobs[pos] = t;
+        } else {
+            uint32_t const pos = atomicAdd(&s_sel[4], 1u);
+            if (GHCM_CHECK(s.ctl, pos < s.num_tiles, 10u)) carry[pos] = t;
+        }
     };
     if (cached) {
 #pragma unroll

@@ -102,7 +102,12 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
 #pragma unroll
         for (int e = 0; e < 4; ++e) sm.queued[e] = kNone;
         s_word[6] = kmx;
-        if (use_tma) {
+        // checked builds: the tile lies in its instance and the box starts on a
+        // 16-byte boundary; otherwise nothing is staged and the job fails
+        bool const tile_ok = GHCM_CHECK(s.ctl, ii < s.num_insts && tc.sx > 0 && tc.sy > 0, 1u);
+        bool const x_ok = GHCM_CHECK(s.ctl, ((tc.ox - 4) & 3) == 0, 2u);
+        s_word[3] = (tile_ok && x_ok) ? 0u : 1u;  // 1: nothing staged (written only here)
+        if (tile_ok && x_ok && use_tma) {
             fence_proxy_async();
             mbar_arrive_expect_tx(bar, static_cast<uint32_t>(2 * G::BOX * sizeof(float)));
             tma_load_2d(sm.time, time_map(s, ii), bar, tc.ox - 4, tc.oy - 2);
@@ -122,7 +127,8 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         __syncthreads();
     }
     bool const vetoed = may_veto && s_word[7] != 0u;
-    if (use_tma) {
+    bool const staged = s_word[3] == 0u;
+    if (use_tma && staged) {
         if (!mbar_wait(bar, parity, s.timeout_ns)) {
             atomicOr(&s.ctl->error, kErrTimeout);
             s_word[1] = 1u;  // every thread acts on it after the barrier below
@@ -133,7 +139,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     }
     if (vetoed) {
         __syncthreads();
-        if (s_word[1]) return kJobFailed;
+        if (s_word[1] || !staged) return kJobFailed;
         if (tid == 0) learn_defer(s, tile, flags, s_word[5], s_word[6], nxt, s_krange);
         __syncthreads();
         return kJobDeferred;
@@ -144,6 +150,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         int const gx = tc.ox + lx, gy = tc.oy + ly;
         int const k = si<B>(lx, ly);
         bool const in = gx >= 0 && gy >= 0 && gx < static_cast<int>(I.w) && gy < static_cast<int>(I.h);
+        if (!GHCM_CHECK(s.ctl, k >= 0 && k < G::BOX, 3u)) continue;
         if (!in) {
             sm.time[k] = f_inf();
             sm.cost[k] = f_inf();
@@ -156,7 +163,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         }
     }
     __syncthreads();
-    if (s_word[1]) return kJobFailed;
+    if (s_word[1] || !staged) return kJobFailed;
 #ifdef GHCM_PROFILE
     uint64_t const p_t1 = (tid == 0) ? global_ns() : 0ull;
 #endif
@@ -172,6 +179,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         lys[k] = id / B;
         inside[k] = lxs[k] < tc.sx && lys[k] < tc.sy;
         idx[k] = si<B>(lxs[k], lys[k]);
+        if (!GHCM_CHECK(s.ctl, idx[k] - BW >= 0 && idx[k] + BW < G::BOX, 4u)) idx[k] = si<B>(0, 0);
         t[k] = sm.time[idx[k]];
         t0[k] = t[k];
         c[k] = sm.cost[idx[k]];
@@ -314,10 +322,12 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
             else if (e == 2) { px = tc.sx; py = ei; qx = tc.sx - 1; qy = ei; fx = tc.sx + 1; fy = ei; }
             else { px = ei; py = tc.sy; qx = ei; qy = tc.sy - 1; fx = ei; fy = tc.sy + 1; }
             int const pi = si<B>(px, py);
-            float const cp = sm.cost[pi];
+            int const fi = si<B>(fx, fy);
+            bool const in_box = GHCM_CHECK(s.ctl, pi - BW >= 0 && pi + BW < G::BOX && fi >= 0 && fi < G::BOX, 5u);
+            float const cp = in_box ? sm.cost[pi] : f_inf();
             if (cp < f_inf()) {
                 float const told = sm.time[pi];
-                float const a_norm = fminf(sm.time[si<B>(qx, qy)], sm.time[si<B>(fx, fy)]);
+                float const a_norm = fminf(sm.time[si<B>(qx, qy)], sm.time[fi]);
                 float const a_lat = (e & 1) ? fminf(sm.time[pi - 1], sm.time[pi + 1])
                                             : fminf(sm.time[pi - BW], sm.time[pi + BW]);
                 float const nt = godunov(a_norm, a_lat, cp, told);
@@ -348,7 +358,8 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     for (int k = 0; k < G::CPT; ++k) {
         if (!inside[k]) continue;
         lmin = fminf(lmin, t[k]);
-        if (tile_changed) I.time[static_cast<size_t>(tc.oy + lys[k]) * I.w + tc.ox + lxs[k]] = t[k];
+        size_t const gi = static_cast<size_t>(tc.oy + lys[k]) * I.w + tc.ox + lxs[k];
+        if (tile_changed && GHCM_CHECK(s.ctl, gi < static_cast<size_t>(I.w) * I.h, 6u)) I.time[gi] = t[k];
     }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
@@ -364,7 +375,8 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         if (capped) activate(s, tile, kFull, m, nxt, s_krange);
     }
     uint32_t const edge_changed = s_word[4];
-    if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u)) {
+    if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u) &&
+        GHCM_CHECK(s.ctl, nb >= 0 && static_cast<uint32_t>(nb) < s.num_tiles, 7u)) {
         if (activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt, s_krange))
             sm.queued[e] = static_cast<uint32_t>(nb);  // appended now: score it (a re-activation keeps its score)
     }
@@ -405,6 +417,7 @@ __device__ void residual_warp(const Sched& s, uint32_t nxt, uint32_t warp_global
             if (lx >= tc.sx || ly >= tc.sy) continue;
             int const gx = tc.ox + lx, gy = tc.oy + ly;
             size_t const gi = static_cast<size_t>(gy) * I.w + gx;
+            if (!GHCM_CHECK(s.ctl, gi < static_cast<size_t>(I.w) * I.h, 8u)) continue;
             float const cst = to_cost(I, __ldg(&I.in[gi]));
             if (!(cst < f_inf())) continue;
             float const t = __ldcg(&I.time[gi]);

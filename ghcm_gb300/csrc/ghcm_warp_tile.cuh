@@ -63,7 +63,9 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
         sm.claim[0] = f;
         sm.claim[1] = kold;
         sm.claim[2] = kmx;
-        if (use_tma) {
+        bool const x_ok = GHCM_CHECK(s.ctl, ((tc.ox - 4) & 3) == 0, 11u);  // x on a 16-byte boundary
+        sm.claim[3] = x_ok ? 1u : 0u;  // 0 (checked builds only): nothing staged, the job fails
+        if (use_tma && x_ok) {
             fence_proxy_async();
             mbar_arrive_expect_tx(&sm.bar, static_cast<uint32_t>(2 * G::BOX * sizeof(float)));
             tma_load_2d(sm.time, time_map(s, ii), &sm.bar, tc.ox - 4, tc.oy - 2);
@@ -73,6 +75,7 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     }
     __syncwarp();
     bool const vetoed = learn_veto_warp(s, tile, sm.claim[0], sm.claim[1], sm.claim[2], wave);
+    if (sm.claim[3] == 0u) return kJobFailed;
     if (use_tma) {
         bool const landed = mbar_wait(&sm.bar, parity, s.timeout_ns);
         parity ^= 1u;
@@ -225,7 +228,8 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
         int const y = band * R + k;
         if (x < tc.sx && y < tc.sy) {
             lmin = fminf(lmin, t[k]);
-            if (tile_changed) I.time[static_cast<size_t>(tc.oy + y) * I.w + tc.ox + x] = t[k];
+            size_t const gi = static_cast<size_t>(tc.oy + y) * I.w + tc.ox + x;
+            if (tile_changed && GHCM_CHECK(s.ctl, gi < static_cast<size_t>(I.w) * I.h, 12u)) I.time[gi] = t[k];
         }
     }
 #pragma unroll
