@@ -399,16 +399,18 @@ int query_persistent(int block, int fim, LaunchInfo* info, bool wide) {
     return 0;
 }
 
-// Enough CTAs per SM that every job of a full wave has a worker of its own,
-// within the occupancy cap. Fewer CTAs make the per-wave grid barrier cheaper
-// and crowd an SM's tile solves less: on the 4096^2 seven-ring field with
-// n = 256, 2 CTAs per SM solved in 13.7 ms against 15.6 ms with 4, while
-// n = 1024, the noise field and batches want all 4.
+// A single field runs the wide build when a full wave holds more than twice
+// as many jobs as the narrow build's grid has CTAs (see kWideCtas).
 bool wide_for(const LaunchInfo& narrow, int sms, uint32_t max_jobs) {
     return static_cast<uint64_t>(max_jobs) >
            2u * static_cast<uint64_t>(std::max(1, narrow.blocks_per_sm)) * static_cast<uint64_t>(std::max(1, sms));
 }
 
+// Enough CTAs per SM that every job of a full wave has a worker of its own,
+// within the occupancy cap. Fewer CTAs make the per-wave grid barrier cheaper
+// and crowd an SM's tile solves less: on the 4096^2 seven-ring field with
+// n = 256, 2 CTAs per SM solved in 13.7 ms against 15.6 ms with 4, while
+// n = 1024, the noise field and batches want all 4.
 int persistent_grid(const LaunchInfo& info, int sms, uint32_t max_jobs) {
     uint64_t const per_round = static_cast<uint64_t>(std::max(1, info.workers)) * static_cast<uint64_t>(sms);
     uint64_t const want = (static_cast<uint64_t>(max_jobs) + per_round - 1u) / per_round;
