@@ -58,6 +58,7 @@ EXPORTS = (
 GHCM_MLP_FEATURES = 12
 GHCM_MLP_HIDDEN = 64
 GHCM_MLP_PARAMS = 5057
+GHCM_REFRESH_OFF = 0xFFFFFFFF
 GHCM_POLICY_SCORE = 0
 GHCM_POLICY_VETO = 1
 
@@ -77,7 +78,8 @@ class GhcmConfig(ctypes.Structure):
         ("use_tma", ctypes.c_uint32),
         ("fallback_jobs", ctypes.c_uint32),
         ("cost_cap", ctypes.c_float),
-        ("reserved", ctypes.c_uint32 * 3),
+        ("refresh_solves", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 2),
     ]
 
 

@@ -27,7 +27,13 @@ enum : uint32_t {
     kFull     = 1u << 1,   // re-solve every cell (residual check, sweep cap)
     kEdgeBit0 = 1u << 4,   // edge e of the tile received new boundary values: kEdgeBit0 << e
     kEdgeMask = 0xFu << 4,
+    kSolveOne = 1u << 8,   // bits 8-11: the tile's block-solves so far, counted up to Sched::refresh
+    kSolveMask = 0xFu << 8,
 };
+constexpr uint32_t kMaxRefresh = 15;  // largest Sched::refresh the 4-bit solve count holds
+constexpr uint32_t kDefaultRefresh = 8;
+
+__host__ __device__ __forceinline__ uint32_t solve_count(uint32_t flags) { return (flags & kSolveMask) >> 8; }
 
 // One eikonal instance: a row-major W x H field and its block tiling.
 struct Inst {
@@ -131,7 +137,8 @@ struct Sched {
     uint32_t  max_sweeps;
     uint32_t  max_waves;
     float     eps;
-    uint32_t  pad0;
+    uint32_t  refresh;             // block-solves per tile that recompute every cell from its neighbours
+                                   // (cells may rise); later solves of the tile only lower cells
     uint64_t  timeout_ns;
     Learn     learn;
 };

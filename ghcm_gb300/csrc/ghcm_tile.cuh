@@ -184,9 +184,20 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         t0[k] = t[k];
         c[k] = sm.cost[idx[k]];
         c2[k] = __fmul_rn(__fmul_rn(c[k], c[k]), 2.0f);
-        v[k] = inside[k] && c[k] < f_inf();
+        v[k] = inside[k] && c[k] < f_inf() && t[k] != 0.f;  // a time of 0 is a seed: fixed
     }
     float const eps = s.eps;
+    // Until the tile has had `refresh` quiet block-solves (solves that moved
+    // no cell far, falls_far), every solve recomputes each cell from its
+    // neighbours, so a cell may rise; after that, and past fresh_sweeps sweeps
+    // within a solve, cells only fall. Rounding makes the update slightly
+    // non-monotone: keeping the minimum of every evaluation (the reference's
+    // form) leaves a cell an ulp low here and there, and along a long front
+    // those ulps add up. Recomputing removes that drift; the budget ends the
+    // one-ulp oscillations of nearly tied neighbours, which only quiet
+    // solves make.
+    bool fresh = solve_count(flags) < s.refresh;
+    uint32_t const fresh_sweeps = 4u * B;
     bool own_changed = false;
     bool capped = false;
     uint32_t sweeps = 0;
@@ -200,9 +211,9 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
                 int const i = idx[k];
                 float const ax = fminf(sm.time[i - 1], sm.time[i + 1]);
                 float const ay = fminf(sm.time[i - BW], sm.time[i + BW]);
-                float const nt = godunov2(ax, ay, c[k], c2[k], t[k]);
-                if (nt < t[k]) {
-                    moved |= time_diff(nt, t[k]) < -eps;
+                float const nt = next_time(godunov2_raw(ax, ay, c[k], c2[k]), t[k], fresh);
+                if (nt != t[k]) {
+                    moved |= moves(nt, t[k], eps, fresh);
                     t[k] = nt;
                     sm.time[i] = nt;
                     own_changed = true;
@@ -210,6 +221,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
             }
             ++sweeps;
             if (!__syncthreads_or(moved)) break;
+            if (sweeps >= fresh_sweeps) fresh = false;
             if (sweeps >= s.max_sweeps) {
                 capped = true;
                 break;
@@ -240,10 +252,10 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
                     int const i = idx[k];
                     float const ax = fminf(sm.time[i - 1], sm.time[i + 1]);
                     float const ay = fminf(sm.time[i - BW], sm.time[i + BW]);
-                    float const nt = godunov2(ax, ay, c[k], c2[k], t[k]);
+                    float const nt = next_time(godunov2_raw(ax, ay, c[k], c2[k]), t[k], fresh);
                     bool moved = false;
-                    if (nt < t[k]) {
-                        moved = time_diff(nt, t[k]) < -eps;
+                    if (nt != t[k]) {
+                        moved = moves(nt, t[k], eps, fresh);
                         t[k] = nt;
                         sm.time[i] = nt;
                         own_changed = true;
@@ -268,9 +280,9 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
                             int const i = idx[k];
                             float const ax = fminf(sm.time[i - 1], sm.time[i + 1]);
                             float const ay = fminf(sm.time[i - BW], sm.time[i + BW]);
-                            float const nt = godunov2(ax, ay, c[k], c2[k], t[k]);
-                            if (nt < t[k]) {
-                                open[k] = time_diff(nt, t[k]) < -eps;
+                            float const nt = next_time(godunov2_raw(ax, ay, c[k], c2[k]), t[k], fresh);
+                            if (nt != t[k]) {
+                                open[k] = moves(nt, t[k], eps, fresh);
                                 t[k] = nt;
                                 sm.time[i] = nt;
                                 own_changed = true;
@@ -281,6 +293,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
                 }
                 ++sweeps;
                 if (!__syncthreads_or(still_open)) break;
+                if (sweeps >= fresh_sweeps) fresh = false;
                 if (sweeps >= s.max_sweeps) {
                     capped = true;
                     break;
@@ -298,6 +311,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
 #pragma unroll
         for (int k = 0; k < G::CPT; ++k) {
             if (!inside[k] || t[k] == t0[k]) continue;
+            if (falls_far(t[k], t0[k])) ec |= 16u;  // not a quiet solve
             if (lxs[k] == 0) ec |= 1u;
             if (lys[k] == 0) ec |= 2u;
             if (lxs[k] == tc.sx - 1) ec |= 4u;
@@ -325,13 +339,14 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
             int const fi = si<B>(fx, fy);
             bool const in_box = GHCM_CHECK(s.ctl, pi - BW >= 0 && pi + BW < G::BOX && fi >= 0 && fi < G::BOX, 5u);
             float const cp = in_box ? sm.cost[pi] : f_inf();
-            if (cp < f_inf()) {
-                float const told = sm.time[pi];
+            float const told = in_box ? sm.time[pi] : 0.f;
+            if (cp < f_inf() && told != 0.f) {  // seeds never change
                 float const a_norm = fminf(sm.time[si<B>(qx, qy)], sm.time[fi]);
                 float const a_lat = (e & 1) ? fminf(sm.time[pi - 1], sm.time[pi + 1])
                                             : fminf(sm.time[pi - BW], sm.time[pi + BW]);
-                float const nt = godunov(a_norm, a_lat, cp, told);
-                if (time_diff(nt, told) < -eps) {
+                bool const track_rise = s.refresh != 0u;
+                float const nt = next_time(godunov_raw(a_norm, a_lat, cp), told, track_rise);
+                if (moves(nt, told, eps, track_rise)) {
                     e_imp = true;
                     e_key = nt;
                 }
@@ -350,7 +365,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     if (s.learn.tstat) {
         bool mv = false;
 #pragma unroll
-        for (int k = 0; k < G::CPT; ++k) mv |= inside[k] && time_diff(t[k], t0[k]) < -eps;
+        for (int k = 0; k < G::CPT; ++k) mv |= inside[k] && moves(t[k], t0[k], eps, true);
         useful = __syncthreads_or(mv) != 0;
     }
     float lmin = f_inf();
@@ -371,6 +386,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         float m = s_red[0];
         for (int w = 1; w < G::THREADS / 32; ++w) m = fminf(m, s_red[w]);
         s.tmin[tile] = m;
+        if (solve_count(flags) < s.refresh && !(s_word[4] & 16u)) atomicAdd(&s.flags[tile], kSolveOne);
         learn_commit(s, tile, useful, wave, sweeps, sm.feat);
         if (capped) activate(s, tile, kFull, m, nxt, s_krange);
     }
@@ -410,6 +426,7 @@ __device__ void residual_warp(const Sched& s, uint32_t nxt, uint32_t warp_global
     for (uint32_t tile = warp_global; tile < s.num_tiles; tile += warps) {
         const Inst& I = s.insts[inst_of(s, tile)];
         TileCoord const tc = tile_coord<B>(I, tile);
+        bool const fresh = solve_count(ld_relaxed(&s.flags[tile])) < s.refresh;
         bool bad = false;
         float kmin = f_inf();
         for (int k = lane; k < B * B; k += 32) {
@@ -421,14 +438,15 @@ __device__ void residual_warp(const Sched& s, uint32_t nxt, uint32_t warp_global
             float const cst = to_cost(I, __ldg(&I.in[gi]));
             if (!(cst < f_inf())) continue;
             float const t = __ldcg(&I.time[gi]);
+            if (t == 0.f) continue;  // seed
             float const xl = gx > 0 ? __ldcg(&I.time[gi - 1]) : f_inf();
             float const xr = gx + 1 < static_cast<int>(I.w) ? __ldcg(&I.time[gi + 1]) : f_inf();
             float const yu = gy > 0 ? __ldcg(&I.time[gi - I.w]) : f_inf();
             float const yd = gy + 1 < static_cast<int>(I.h) ? __ldcg(&I.time[gi + I.w]) : f_inf();
-            float const nt = godunov(fminf(xl, xr), fminf(yu, yd), cst, t);
-            if (time_diff(nt, t) < -s.eps) {
+            float const nt = next_time(godunov_raw(fminf(xl, xr), fminf(yu, yd), cst), t, fresh);
+            if (moves(nt, t, s.eps, fresh)) {
                 bad = true;
-                kmin = fminf(kmin, nt);
+                kmin = fminf(kmin, fminf(nt, t));
             }
         }
         if (__any_sync(0xffffffffu, bad)) {

@@ -109,16 +109,21 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     __syncwarp();
 
     float t[R], c[R], c2[R];
+    bool fix[R];  // seeds (time 0) and walls keep their value
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         int const i = si<B>(x, band * R + k);
         t[k] = sm.time[i];
         c[k] = sm.cost[i];
         c2[k] = __fmul_rn(__fmul_rn(c[k], c[k]), 2.0f);
+        fix[k] = t[k] == 0.f || !(c[k] < f_inf());
     }
     float const h_top = sm.time[si<B>(x, -1)];  // used by band 0
     float const h_bot = sm.time[si<B>(x, B)];   // used by the last band
     float const eps = s.eps;
+    // until the tile has had `refresh` quiet block-solves it recomputes its cells (see solve_tile)
+    bool fresh = solve_count(sm.claim[0]) < s.refresh;
+    uint32_t const fresh_sweeps = 4u * B;
     bool changed = false;
     bool capped = false;
     uint32_t sweeps = 0;
@@ -135,16 +140,17 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
             if (x == B - 1) r = sm.time[si<B>(B, band * R + k)];
             float const u = (k > 0) ? t[k > 0 ? k - 1 : 0] : (band > 0 ? up_in : h_top);
             float const d = (k < R - 1) ? t[k < R - 1 ? k + 1 : 0] : (band < W::G - 1 ? down_in : h_bot);
-            nt[k] = godunov2(fminf(l, r), fminf(u, d), c[k], c2[k], t[k]);
-            moved |= time_diff(nt[k], t[k]) < -eps;
+            nt[k] = fix[k] ? t[k] : next_time(godunov2_raw(fminf(l, r), fminf(u, d), c[k], c2[k]), t[k], fresh);
+            moved |= moves(nt[k], t[k], eps, fresh);
         }
 #pragma unroll
         for (int k = 0; k < R; ++k) {
-            changed |= nt[k] < t[k];
+            changed |= nt[k] != t[k];
             t[k] = nt[k];
         }
         ++sweeps;
         if (!__any_sync(FULL, moved)) break;
+        if (sweeps >= fresh_sweeps) fresh = false;
         if (sweeps >= s.max_sweeps) {
             capped = true;
             break;
@@ -160,7 +166,8 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
         int const y = band * R + k;
         float const staged = sm.time[si<B>(x, y)];
         sm.time[si<B>(x, y)] = t[k];
-        mv |= x < tc.sx && y < tc.sy && time_diff(t[k], staged) < -eps;
+        mv |= x < tc.sx && y < tc.sy && moves(t[k], staged, eps, true);
+        if (x < tc.sx && y < tc.sy && t[k] != staged && falls_far(t[k], staged)) ec |= 16u;  // not a quiet solve
         if (x < tc.sx && y < tc.sy && t[k] != staged) {
             if (x == 0) ec |= 1u;
             if (y == 0) ec |= 2u;
@@ -191,13 +198,14 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
             else { px = ei; py = tc.sy; qx = ei; qy = tc.sy - 1; fx = ei; fy = tc.sy + 1; }
             int const pi = si<B>(px, py);
             float const cp = sm.cost[pi];
-            if (cp < f_inf()) {
-                float const told = sm.time[pi];
+            float const told = sm.time[pi];
+            if (cp < f_inf() && told != 0.f) {  // seeds never change
                 float const a_norm = fminf(sm.time[si<B>(qx, qy)], sm.time[si<B>(fx, fy)]);
                 float const a_lat = (e & 1) ? fminf(sm.time[pi - 1], sm.time[pi + 1])
                                             : fminf(sm.time[pi - G::BW], sm.time[pi + G::BW]);
-                float const nv = godunov(a_norm, a_lat, cp, told);
-                if (time_diff(nv, told) < -eps) {
+                bool const track_rise = s.refresh != 0u;
+                float const nv = next_time(godunov_raw(a_norm, a_lat, cp), told, track_rise);
+                if (moves(nv, told, eps, track_rise)) {
                     imp = true;
                     key = nv;
                 }
@@ -238,6 +246,7 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     __syncwarp();
     if (lane == 0) {
         s.tmin[tile] = lmin;
+        if (solve_count(sm.claim[0]) < s.refresh && !(ec & 16u)) atomicAdd(&s.flags[tile], kSolveOne);
         learn_commit(s, tile, useful, wave, sweeps, sm.feat);
 #pragma unroll
         for (int e = 0; e < 4; ++e)

@@ -69,6 +69,7 @@ class HcmConfig:
     device: int = -1
     fallback_jobs: int = 0                 # learned schedule: n of a wave in which no tile qualifies
     cost_cap: float = 0.0                  # > 0: cost = min(cost, cost_cap) (field_cost_as_permeable)
+    refresh_solves: int = 0                # solves per tile that recompute cells (0 = 8; _lib.GHCM_REFRESH_OFF = none)
 
     def to_c(self, sm_count: int | None = None) -> GhcmConfig:
         c = GhcmConfig()
@@ -89,6 +90,7 @@ class HcmConfig:
         c.use_tma = 1 if self.use_tma else 0
         c.fallback_jobs = int(self.fallback_jobs)
         c.cost_cap = float(self.cost_cap)
+        c.refresh_solves = int(self.refresh_solves)
         return c
 
 

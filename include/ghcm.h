@@ -50,6 +50,10 @@ extern "C" {
 #define GHCM_SCHEDULE_PLAIN   0    /* lowest-key-first top-n (the reference's priority queue) */
 #define GHCM_SCHEDULE_LEARNED 1    /* learned block-scheduling score */
 
+/* ghcm_config.refresh_solves: no block-solve recomputes cells; every update keeps
+ * min(T_old, update) */
+#define GHCM_REFRESH_OFF 0xFFFFFFFFu
+
 /* ghcm_config.key_mode - the plain priority key */
 #define GHCM_KEY_BOUNDARY_MIN 0    /* min arrival time among the boundary values that activated the tile */
 #define GHCM_KEY_BLOCK_MIN    1    /* min smallest_time over the tile and its 4 neighbours
@@ -73,7 +77,12 @@ typedef struct ghcm_config {
     float    cost_cap;        /* > 0: cost = min(cost, cost_cap), the reference's permeable-wall
                                  transform field_cost_as_permeable (src/test_runner.cpp:70-75,
                                  default there 1e3); 0 = no cap */
-    uint32_t reserved[3];     /* must be zero */
+    uint32_t refresh_solves;  /* block-solves of each tile that recompute every cell from its
+                                 neighbours, so a cell may rise; the tile's later solves only lower
+                                 cells, as the reference's min(T_old, update) does
+                                 (data/eikonal_common.cl:288-308). 0 = 8; 1..15; GHCM_REFRESH_OFF =
+                                 none (every update keeps the minimum) */
+    uint32_t reserved[2];     /* must be zero */
 } ghcm_config;
 
 typedef struct ghcm_stats {

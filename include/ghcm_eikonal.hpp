@@ -85,6 +85,7 @@ struct HcmConfig {
     uint32_t max_waves = 0;
     uint32_t wait_timeout_ms = 2000;
     bool use_tma = true;
+    uint32_t refresh_solves = 0;          // solves per tile that recompute cells (0 = 8, GHCM_REFRESH_OFF = none)
 };
 
 struct EikonalResult {
@@ -117,6 +118,7 @@ inline ghcm_config to_c(HcmConfig const& c, uint32_t sms, int device) {
     out.wait_timeout_ms = c.wait_timeout_ms;
     out.device = device;
     out.use_tma = c.use_tma ? 1u : 0u;
+    out.refresh_solves = c.refresh_solves;
     return out;
 }
 

@@ -68,7 +68,7 @@ def test_defaults_mirror_the_reference_config(ghcm_lib):
     assert c.block_size == 16 and c.max_jobs == 0
     assert abs(c.eps - 1e-5) < 1e-12  # HcmConfig::fim_minimum_change (src/eikonal.h:24)
     assert c.kernel == _lib.GHCM_KERNEL_SYSTOLIC  # HcmConfig::kernel (src/eikonal.h:26)
-    assert c.use_tma == 1 and c.device == -1 and c.fallback_jobs == 0 and c.cost_cap == 0.0 and list(c.reserved) == [0] * 3
+    assert c.use_tma == 1 and c.device == -1 and c.fallback_jobs == 0 and c.cost_cap == 0.0 and c.refresh_solves == 0 and list(c.reserved) == [0] * 2
 
 
 def test_status_strings(ghcm_lib):
@@ -82,12 +82,12 @@ def test_create_rejects_bad_config(ghcm_lib):
     c = _lib.GhcmConfig()
     ghcm_lib.ghcm_config_default(ctypes.byref(c))
     h = ctypes.c_void_p()
-    for field, value in (("block_size", 12), ("kernel", 7), ("eps", -1.0)):
+    for field, value in (("block_size", 12), ("kernel", 7), ("eps", -1.0), ("refresh_solves", 16)):
         bad = _lib.GhcmConfig.from_buffer_copy(c)
         setattr(bad, field, value)
         assert ghcm_lib.ghcm_create(ctypes.byref(bad), ctypes.byref(h)) == _lib.GHCM_ERR_BAD_ARG
     bad = _lib.GhcmConfig.from_buffer_copy(c)
-    bad.reserved[2] = 1
+    bad.reserved[1] = 1
     assert ghcm_lib.ghcm_create(ctypes.byref(bad), ctypes.byref(h)) == _lib.GHCM_ERR_BAD_ARG
     assert ghcm_lib.ghcm_create(None, ctypes.byref(h)) == _lib.GHCM_ERR_BAD_ARG
 
