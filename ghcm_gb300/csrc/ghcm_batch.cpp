@@ -52,7 +52,8 @@ int check_instance(const ghcm_instance& in) {
     if (!in.field || !in.time_out || in.width == 0 || in.height == 0) return GHCM_ERR_BAD_ARG;
     if (in.n_seeds && !in.seeds_xy) return GHCM_ERR_BAD_ARG;
     if (!(in.h > 0.f) || !std::isfinite(in.h) || in.reserved != 0u) return GHCM_ERR_BAD_ARG;
-    if (static_cast<uint64_t>(in.width) * in.height > (1ull << 34)) return GHCM_ERR_UNSUPPORTED;
+    if (in.width > kMaxSide || in.height > kMaxSide || static_cast<uint64_t>(in.width) * in.height > (1ull << 34))
+        return GHCM_ERR_UNSUPPORTED;
     return GHCM_OK;
 }
 
@@ -60,7 +61,7 @@ int check_instance(const ghcm_instance& in) {
 cudaError_t enqueue(ghcm_batch* b, cudaStream_t st) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(b->s.ctl, 0, sizeof(Ctl), st)) != cudaSuccess) return e;
-    if ((e = launch_init(b->s, b->count, b->max_cells, b->max_seeds, static_cast<int>(b->cfg.block_size), st)) !=
+    if ((e = launch_init(b->s, b->count, b->max_cells, b->max_seeds, static_cast<int>(b->cfg.block_size), b->sms, st)) !=
         cudaSuccess)
         return e;
     if ((e = launch_persistent(static_cast<int>(b->cfg.block_size), b->cfg.kernel == GHCM_KERNEL_FIM, b->s, b->grid,

@@ -93,7 +93,8 @@ Layout layout_for(uint32_t tiles, uint32_t jobs) {
 int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t w, uint32_t h, float spacing,
               const uint32_t* d_seeds, uint32_t n_seeds, float* d_time, cudaStream_t st, ghcm_stats* stats) {
     uint32_t const B = ctx->cfg.block_size;
-    uint32_t const tx = (w + B - 1) / B, ty = (h + B - 1) / B;
+    if (w > kMaxSide || h > kMaxSide) return GHCM_ERR_UNSUPPORTED;
+    uint32_t const tx = (w + B - 1) / B, ty = (h + B - 1) / B;  // no wrap: w, h <= kMaxSide
     uint64_t const tiles64 = static_cast<uint64_t>(tx) * ty;
     if (tiles64 >= (1ull << 31)) return GHCM_ERR_UNSUPPORTED;
     uint32_t const tiles = static_cast<uint32_t>(tiles64);
@@ -160,7 +161,7 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
         return map_cuda(e);
     if ((e = cudaMemsetAsync(s.ctl, 0, sizeof(Ctl), st)) != cudaSuccess) return map_cuda(e);
     cudaEventRecord(ctx->ev0, st);
-    if ((e = launch_init(s, 1, static_cast<uint64_t>(w) * h, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
+    if ((e = launch_init(s, 1, static_cast<uint64_t>(w) * h, n_seeds, static_cast<int>(B), ctx->sms, st)) != cudaSuccess)
         return map_cuda(e);
     // the wide build for plain waves of many jobs; the learned schedule stays on
     // the 4-CTA build, where its scoring ran 7.2 ms against 9.0 ms on the wide
@@ -206,7 +207,7 @@ int check_field_args(ghcm_ctx* ctx, const void* field, uint32_t w, uint32_t h, f
     if (!ctx || !field || !out || w == 0 || h == 0) return GHCM_ERR_BAD_ARG;
     if (n_seeds && !seeds) return GHCM_ERR_BAD_ARG;
     if (!(spacing > 0.f) || !std::isfinite(spacing)) return GHCM_ERR_BAD_ARG;
-    if (static_cast<uint64_t>(w) * h > (1ull << 34)) return GHCM_ERR_UNSUPPORTED;
+    if (w > kMaxSide || h > kMaxSide || static_cast<uint64_t>(w) * h > (1ull << 34)) return GHCM_ERR_UNSUPPORTED;
     return GHCM_OK;
 }
 

@@ -68,6 +68,11 @@ inline int map_cuda(cudaError_t e) {
     return GHCM_ERR_CUDA;
 }
 
+// Largest field side the solver accepts. Tile origins and staged-box
+// coordinates are 32-bit signed in the kernels, and a side this size keeps
+// side + B - 1 and every coordinate far from overflowing them.
+constexpr uint32_t kMaxSide = 1u << 30;
+
 // Ctl::error bits -> status, most specific first.
 inline int status_from_error(uint32_t error) {
     if (error & kErrBadSeed) return GHCM_ERR_BAD_ARG;

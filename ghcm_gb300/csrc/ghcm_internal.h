@@ -173,7 +173,7 @@ bool wide_for(const LaunchInfo& narrow, int sms, uint32_t max_jobs);
 void tile_box(int block, uint32_t* width, uint32_t* height);
 // Initialises the per-tile state, the time fields (+inf, inputs checked) and
 // the seeds of every instance. max_cells / max_seeds: the largest instance.
-cudaError_t launch_init(const Sched& s, uint32_t n_insts, uint64_t max_cells, uint32_t max_seeds, int block,
+cudaError_t launch_init(const Sched& s, uint32_t n_insts, uint64_t max_cells, uint32_t max_seeds, int block, int sms,
                         cudaStream_t st);
 cudaError_t launch_persistent(int block, int fim, const Sched& s, int grid, cudaStream_t st, bool wide = false);
 cudaError_t launch_wait_selftest(uint32_t* flag, Ctl* ctl, uint64_t timeout_ns, cudaStream_t st);

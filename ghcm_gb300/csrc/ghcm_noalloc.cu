@@ -77,8 +77,9 @@ extern "C" int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_
     if (!d_field || !d_time_out || width == 0 || height == 0 || (n_seeds && !d_seeds_xy)) return GHCM_ERR_BAD_ARG;
     if (!(h > 0.f) || !(h < 3.0e38f)) return GHCM_ERR_BAD_ARG;
     uint32_t const B = cfg->block_size;
-    uint64_t const tiles64 = static_cast<uint64_t>((width + B - 1) / B) * ((height + B - 1) / B);
-    if (tiles64 > GHCM_NOALLOC_MAX_TILES) return GHCM_ERR_TOO_LARGE;
+    // tile counts in 64 bits: (width + B - 1) in 32 bits wraps for widths near 2^32
+    uint64_t const tiles64 = ((static_cast<uint64_t>(width) + B - 1) / B) * ((static_cast<uint64_t>(height) + B - 1) / B);
+    if (tiles64 > GHCM_NOALLOC_MAX_TILES || width > kMaxSide || height > kMaxSide) return GHCM_ERR_TOO_LARGE;
     uint32_t const tiles = static_cast<uint32_t>(tiles64);
 
     int dev = 0;
@@ -136,7 +137,7 @@ extern "C" int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_
     k_store_inst<<<1, 1, 0, st>>>(d_inst, inst);
     if ((e = cudaGetLastError()) != cudaSuccess) return GHCM_ERR_CUDA;
     if ((e = cudaMemsetAsync(s.ctl, 0, sizeof(Ctl), st)) != cudaSuccess) return GHCM_ERR_CUDA;
-    if ((e = launch_init(s, 1, static_cast<uint64_t>(width) * height, n_seeds, static_cast<int>(B), st)) != cudaSuccess)
+    if ((e = launch_init(s, 1, static_cast<uint64_t>(width) * height, n_seeds, static_cast<int>(B), sms, st)) != cudaSuccess)
         return GHCM_ERR_CUDA;
     LaunchInfo wl{};
     if (wide_for(li, sms, s.max_jobs) &&
@@ -146,9 +147,12 @@ extern "C" int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_
                                li.wide)) !=
         cudaSuccess)
         return GHCM_ERR_CUDA;
-    uint32_t error = 0u;
-    if ((e = cudaMemcpyAsync(&error, &s.ctl->error, sizeof(error), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    // the whole control block back (error bits, and the failing site id of an
+    // index check in GHCM_CHECKED builds)
+    Ctl c;
+    if ((e = cudaMemcpyAsync(&c, s.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return GHCM_ERR_CUDA;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return GHCM_ERR_CUDA;
-    return status_from_error(error);
+    report_checks(c);
+    return status_from_error(c.error);
 }

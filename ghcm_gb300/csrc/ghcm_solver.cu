@@ -418,17 +418,17 @@ int persistent_grid(const LaunchInfo& info, int sms, uint32_t max_jobs) {
     return per_sm * sms;
 }
 
-cudaError_t launch_init(const Sched& s, uint32_t n_insts, uint64_t max_cells, uint32_t max_seeds, int block,
+cudaError_t launch_init(const Sched& s, uint32_t n_insts, uint64_t max_cells, uint32_t max_seeds, int block, int sms,
                         cudaStream_t st) {
-    if (n_insts == 0u || n_insts > 65535u) return cudaErrorInvalidValue;
+    if (n_insts == 0u || n_insts > 65535u || sms <= 0) return cudaErrorInvalidValue;
     unsigned const tb = 256;
     // about 16 CTAs per SM over the whole batch, at least 8 per instance
     uint64_t const want = (max_cells + tb - 1) / tb;
-    unsigned const per = static_cast<unsigned>(std::max<uint64_t>(8u, 152u * 16u * 4u / n_insts));
+    unsigned const per = static_cast<unsigned>(std::max<uint64_t>(8u, static_cast<uint64_t>(sms) * 16u * 4u / n_insts));
     unsigned const gx = static_cast<unsigned>(std::max<uint64_t>(1u, std::min<uint64_t>(want, per)));
     k_init_inst<<<dim3(gx, n_insts), tb, 0, st>>>(s);
     if (s.learn.tstat) {
-        unsigned const g = static_cast<unsigned>(std::min<uint32_t>((s.num_tiles + 7u) / 8u, 152u * 16u));
+        unsigned const g = static_cast<unsigned>(std::min<uint32_t>((s.num_tiles + 7u) / 8u, static_cast<uint32_t>(sms) * 16u));
         switch (block) {
             case 8: k_tile_stats<8><<<g, tb, 0, st>>>(s); break;
             case 16: k_tile_stats<16><<<g, tb, 0, st>>>(s); break;

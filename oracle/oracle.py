@@ -20,7 +20,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "libghcm_oracle.so"
 REF_SO = HERE / "_ref" / "libghcm_ref.so"
-REF_SRC = Path(os.environ.get("GHCM_REF_SRC", "/root/reference/src"))
+# the reference checkout beside this repository, or GHCM_REF_SRC
+REF_SRC = Path(os.environ.get("GHCM_REF_SRC", HERE.parent.parent / "reference" / "src"))
 
 _f32p = ctypes.POINTER(ctypes.c_float)
 _f64p = ctypes.POINTER(ctypes.c_double)

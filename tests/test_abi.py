@@ -168,3 +168,15 @@ def test_cost_cap_must_be_a_non_negative_number(ghcm_lib):
         x = _lib.GhcmConfig.from_buffer_copy(c)
         x.cost_cap = bad
         assert ghcm_lib.ghcm_create(ctypes.byref(x), ctypes.byref(h)) == _lib.GHCM_ERR_BAD_ARG
+
+
+def test_noalloc_rejects_sizes_that_wrap_before_any_launch(ghcm_lib):
+    """A width near 2^32 must not wrap the tile count to a small number: the
+    call returns GHCM_ERR_TOO_LARGE before touching the device (so this runs
+    without a GPU, with dummy pointers that are never dereferenced)."""
+    c = _lib.GhcmConfig()
+    ghcm_lib.ghcm_config_default(ctypes.byref(c))
+    dummy = ctypes.c_void_p(16)
+    for w, h in ((0xFFFFFFFF, 1), (1, 0xFFFFFFFF), (0xFFFFFFF1, 0xFFFFFFF1), (1 << 31, 2)):
+        rc = ghcm_lib.ghcm_solve_device_noalloc(ctypes.byref(c), dummy, 1, w, h, 1.0, dummy, 1, dummy, None)
+        assert rc == _lib.GHCM_ERR_TOO_LARGE, (w, h, rc)

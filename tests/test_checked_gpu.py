@@ -3,8 +3,8 @@ the tile solvers, the residual pass and the top-n gather compute is checked
 (a failed check sets an error bit and skips the access; the solve returns
 GHCM_ERR_INTERNAL and names the site on stderr). Small and odd grid sizes,
 every tile size, both tile kernels, TMA and plain staging, batches (the
-8-CTA-per-SM builds) and a single field with many jobs per wave must pass
-every check and still match the oracle FIM.
+8-CTA-per-SM builds), a single field with many jobs per wave and the no-alloc
+entry point must pass every check and still match the oracle FIM.
 
 The checked library is built in-tree and run in a child process, so that its
 handles never mix with those of the library the other tests load.
@@ -69,6 +69,23 @@ for block in (16, 32):
     for di, (_, _, r) in zip(insts, cases):
         worst = max(worst, rel_diff(di.d_time.cpu().numpy(), r))
         runs += 1
+# the no-alloc entry point on one small odd-size field
+import ctypes
+speed, seeds, ref = cases[3]
+cfg = _lib.GhcmConfig()
+_lib._lib.ghcm_config_default(ctypes.byref(cfg))
+cfg.block_size = 16
+cfg.max_jobs = 16
+d_speed = torch.from_numpy(speed).to(dev)
+d_seeds = torch.from_numpy(seeds.astype(np.int32)).to(dev)
+d_time = torch.empty_like(d_speed)
+rc = _lib._lib.ghcm_solve_device_noalloc(ctypes.byref(cfg), ctypes.c_void_p(d_speed.data_ptr()), 1, speed.shape[1],
+                                          speed.shape[0], 1.0, ctypes.c_void_p(d_seeds.data_ptr()), seeds.shape[0],
+                                          ctypes.c_void_p(d_time.data_ptr()),
+                                          ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+assert rc == 0, rc
+worst = max(worst, rel_diff(d_time.cpu().numpy(), ref))
+runs += 1
 print(json.dumps({{"worst": worst, "runs": runs}}))
 """
 
@@ -80,5 +97,5 @@ def test_checked_build_passes_every_index_check(cuda_ok):
     assert r.returncode == 0, r.stderr[-3000:]
     assert "[ghcm-checked]" not in r.stderr
     d = json.loads(r.stdout.strip().splitlines()[-1])
-    assert d["runs"] == 5 * 3 * 2 * 2 + 1 + 2 * 5
+    assert d["runs"] == 5 * 3 * 2 * 2 + 1 + 2 * 5 + 1
     assert d["worst"] <= TOL
