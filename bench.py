@@ -1,32 +1,38 @@
 """Benchmark of the gHCM block eikonal solve on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ghcm|reference]
-                    [--workload ring|batched]
+                    [--workload noise|ring|batched|maze]
 
 Default workload (one "step" = one solve to convergence): the 4096 x 4096
-seven-ring speed field (radii 256..1920, barrier width 16, speed 0.01, 64-cell
-gaps at seeded angles, one centre source, h = 1), tiles of 16 x 16, the plain
-device top-n schedule with n = 256 (the configuration's other n, 1024 and
-4096, are timed and reported beside it), eps = 1e-5. Synthetic, seeded input:
-the reference's ring images are replaced by the same construction drawn
-procedurally. Beside it the line reports the error of the field against an
-FP64 FMM, and the learned schedule against the plain one on the 4096 x 4096
-fractal-noise field with 16 sources (model file from
-ghcm_gb300/train_schedule.py, trained on 32 other seeds).
+fractal value-noise speed field (6 octaves, base period 512, persistence 0.5,
+speed = clamp(exp(2 noise), 0.02, 1)) with 16 sources, seed 1, h = 1, tiles of
+16, eps = 1e-5, solved by the LEARNED block schedule (the 12-64-64-1 MLP of
+ghcm_gb300/models/, trained on traces of the plain solver on 32 other seeds;
+score policy, at most 4096 jobs a wave, filled to 1024 in key order). `value`
+is its Mcell/s; the PLAIN device schedule (n = 1024) is timed the same way in
+the same run and reported beside it (`plain`, `learned_vs_plain`), with the
+other plain n and the veto policy under `others`. Both fields are checked
+against the reference's CPU FIM and FMM (oracle restatements, bit-exact to the
+reference build) and an FP64 FMM. Sub-objects: `ring_4096` - the 4096 x 4096
+seven-ring field (radii 256..1920, barrier width 16, speed 0.01, 64-cell gaps,
+one centre source) with the plain schedule at n = 256, 1024, 4096 - and
+`small_ring_256` (the 256 x 256 ring, B = 8, n = 64). Synthetic, seeded input.
 
+--workload ring: the seven-ring field as the headline (plain schedule, --n).
 --workload batched: 512 independent instances (side log-uniform in
 [64, 1024], multiples of 16, seven-ring or noise, 1-8 sources) in one
 persistent launch replayed from a CUDA graph, tile size / n / sweep cap from
 the autotuner; with N ranks the instances are split by cells (weak scaling).
+--workload maze: the 16384 x 16384 cellular-automaton maze, 64 sources.
 
 Metric: Mcell/s to convergence = cells / (time from device-resident speed and
 seeds to the device-resident converged time field). `value` is that, summed
-over all ranks; `e2e` is the same metric through the public calls with the
-host<->device copies of inputs and results inside the timed region.
+over all ranks; `e2e` is the same metric through the public host-pointer call
+with the host<->device copies of inputs and results inside the timed region.
 
 --impl reference times the reference's CPU solver (the FMM of
 src/eikonal_fmm.cpp as restated in oracle/, bit-exact to the reference build)
-on the same workload, over the host's cores.
+on the same workload, one full solve per host thread per step.
 """
 from __future__ import annotations
 
@@ -48,7 +54,8 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Mcell/s to convergence, learned vs plain schedule, 1 GB300, max rel err \u22641e-5"
 UNIT = "Mcell/s"
-WORKLOAD = "ring7_4096x4096"
+WORKLOAD = "noise_4096x4096_16src"
+RING_WORKLOAD = "ring7_4096x4096"
 BATCH_WORKLOAD = "batched_512_ring7_or_noise_64_to_1024"
 MAZE_WORKLOAD = "ca_maze_16384x16384_64src"
 MAZE_SEED = 5
@@ -58,9 +65,13 @@ BATCH_SEED = 1234
 NOISE_EVAL_SEED = 1
 MODEL = ROOT / "ghcm_gb300" / "models" / "schedule_noise4096_b16.npz"
 LAUNCHES_PER_SOLVE = 3  # k_init_inst, k_init_seeds, the persistent k_solve
+LAUNCHES_PER_LEARNED_SOLVE = 4  # the same and k_tile_stats (the learned features' per-tile speed statistics)
 BLOCK = 16
-N_JOBS = 256
+N_JOBS = 256  # the seven-ring workload's headline n
 N_SWEEP = (256, 1024, 4096)
+LEARNED_CAPS = {"max_jobs": 4096, "fallback_jobs": 1024}  # the learned schedule's jobs per wave: cap, plain fill
+PLAIN_N = 1024  # the plain schedule the learned one is compared with (the fastest n on this field)
+PLAIN_SWEEP = (512, 1024, 2048, 4096)
 EPS = 1e-5
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB of L2
 
@@ -70,10 +81,16 @@ def bytes_per_solve(b: int) -> int:
     return 4 * b * b + 4 * ((b + 2) * (b + 2) - 4) + 4 * b * b
 
 
-def make_workload():
+def make_workload(kind: str = "noise"):
+    """The headline field: 4096^2 fractal value noise (6 octaves, base period
+    512, persistence 0.5, speed = clamp(exp(2 noise), 0.02, 1)), 16 sources,
+    seed NOISE_EVAL_SEED (not among the schedule model's training seeds); or
+    the 4096^2 seven-ring field."""
     from ghcm_gb300 import fields
 
-    return fields.ring7_large(seed=1)
+    if kind == "ring":
+        return fields.ring7_large(seed=1)
+    return fields.value_noise(4096, seed=NOISE_EVAL_SEED, base_period=512.0, sources=16)
 
 
 def dist_env():
@@ -247,7 +264,7 @@ def run_reference(args, world, rank) -> int:
         }
         print(json.dumps(line), flush=True)
         return 0
-    speed, seeds = make_workload()
+    speed, seeds = make_workload(args.workload)
     cost = fields.cost_from_speed(speed)
     # a step: one full solve of the workload on every host thread at once
     threads = max(1, os.cpu_count() or 1)
@@ -259,8 +276,8 @@ def run_reference(args, world, rank) -> int:
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": us / 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "solver": "reference FMM (src/eikonal_fmm.cpp), CPU",
-                   "threads": threads},
+        "config": {"workload": RING_WORKLOAD if args.workload == "ring" else WORKLOAD,
+                   "solver": "reference FMM (src/eikonal_fmm.cpp), CPU", "threads": threads},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} step(s) of {threads} concurrent full solves of the workload, "
                                    "one per host thread"},
@@ -340,66 +357,53 @@ def reference_schedule(o, cost, seeds, block: int, n: int, wg: int, fim) -> dict
             "note": "CPU restatement; the wave's jobs run one after another"}
 
 
-def learned_vs_plain(g, dev, stream, flush, steps: int, warmup: int, fp64: bool = True) -> dict:
-    """The learned schedule against the plain one on the 4096^2 noise field
-    (16 sources, seed NOISE_EVAL_SEED, not among the model's training seeds)."""
+def _learned_setup(g, learned, params, threshold, policy, **kw):
+    cfg = g.HcmConfig(block_size=BLOCK, fim_minimum_change=EPS, schedule=g.Schedule.Learned, **kw)
+    s = g.HcmSetup(cfg)
+    learned.set_model(s, params, threshold)
+    learned.set_policy(s, policy)
+    return s
+
+
+def ring_4096(g, dev, stream, flush, steps: int, warmup: int, checks: bool) -> dict:
+    """The plain device schedule at scale: the 4096^2 seven-ring field (radii
+    256..1920, width 16, speed 0.01, 64-cell gaps, one centre source), tiles of
+    16, n in {256, 1024, 4096}, device-resident and timed like the headline,
+    with its parity against the reference FIM and FMM and its error against
+    the FP64 FMM."""
     import torch
 
-    from ghcm_gb300 import fields, learned
-    from oracle.oracle import rel_diff
+    from ghcm_gb300 import fields
+    from oracle.oracle import Oracle, build, rel_diff
 
-    if not MODEL.exists():
-        return {"unavailable": f"no model file {MODEL.name}: python -m ghcm_gb300.train_schedule writes it"}
-    params, threshold, meta = learned.load_model(MODEL)
-    speed, seeds = fields.value_noise(4096, seed=NOISE_EVAL_SEED, base_period=512.0, sources=16)
+    speed, seeds = fields.ring7_large(seed=1)
     cells = speed.size
     d_speed = torch.from_numpy(speed).to(dev)
     d_seeds = torch.from_numpy(seeds.astype(np.int32)).to(dev)
-    runs = {
-        "plain_n1024": (g.HcmConfig(block_size=16, max_jobs=1024, fim_minimum_change=EPS), None),
-        "plain_n4096": (g.HcmConfig(block_size=16, max_jobs=4096, fim_minimum_change=EPS), None),
-        "learned_score_fb1024": (g.HcmConfig(block_size=16, max_jobs=4096, fallback_jobs=1024,
-                                             fim_minimum_change=EPS, schedule=g.Schedule.Learned), learned.POLICY_SCORE),
-        "learned_veto_n1024": (g.HcmConfig(block_size=16, max_jobs=1024, fim_minimum_change=EPS,
-                                           schedule=g.Schedule.Learned), learned.POLICY_VETO),
-    }
-    out, fields_out = {}, {}
-    for name, (cfg, policy) in runs.items():
+    out, fields_out = {"workload": RING_WORKLOAD, "block": BLOCK}, {}
+    for n in N_SWEEP:
         d_time = torch.empty_like(d_speed)
-        with g.HcmSetup(cfg) as s:
-            if policy is not None:
-                learned.set_model(s, params, threshold)
-                learned.set_policy(s, policy)
+        with g.HcmSetup(g.HcmConfig(block_size=BLOCK, max_jobs=n, fim_minimum_change=EPS)) as s:
             ms, sts = timed_device_solves(g, s, d_speed, d_seeds, d_time, stream, flush, steps, warmup)
-            c = learned.counters(s) if policy is not None else {}
-        fields_out[name] = d_time.cpu().numpy()
-        out[name] = {"mcells": cells / (ms * 1e3), "ms": ms,
-                     "block_solves": statistics.mean(x["block_solves"] for x in sts),
-                     "waves": statistics.mean(x["waves"] for x in sts), **c}
-    base = out["plain_n1024"]["block_solves"]
-    ref64 = None
-    if fp64:  # the accuracy oracle: FMM in FP64 (checker only)
-        from oracle.oracle import Oracle, build
-
+        fields_out[n] = d_time.cpu().numpy()
+        out[f"n{n}"] = {"mcells": cells / (ms * 1e3), "ms": ms,
+                        "kernel_ms": statistics.mean(x["kernel_ms"] for x in sts),
+                        "block_solves": statistics.mean(x["block_solves"] for x in sts),
+                        "waves": statistics.mean(x["waves"] for x in sts)}
+    if checks:
         build(with_reference=False)
-        ref64, _ = Oracle().fmm64(fields.cost_from_speed(speed), seeds)
-    ref_sched = None
-    if fp64:  # the reference's own schedule, restated on the CPU (checker only)
         o = Oracle()
         cost = fields.cost_from_speed(speed)
-        ref_sched = reference_schedule(o, cost, seeds, 16, 1024, 256, o.fim(cost, seeds, EPS)[0])
-    for name in runs:
-        out[name]["solves_vs_plain_n1024"] = out[name]["block_solves"] / base
-        out[name]["max_rel_vs_plain_n1024"] = rel_diff(fields_out[name], fields_out["plain_n1024"])
-        if ref64 is not None:
-            out[name]["vs_fmm64"] = fmm64_errors(fields_out[name], ref64)
-        if ref_sched is not None:
-            out[name]["solves_vs_reference_schedule"] = out[name]["block_solves"] / ref_sched["block_solves"]
-    res = {"workload": "noise_4096x4096_16src", "seed": NOISE_EVAL_SEED, "threshold": threshold,
-           "model": MODEL.name, "train_seeds": int(len(meta.get("train_seeds", []))), "runs": out}
-    if ref_sched is not None:
-        res["reference_schedule_n1024"] = ref_sched
-    return res
+        fim, us_fim = o.fim(cost, seeds, EPS)
+        fmm, us_fmm = o.fmm(cost, seeds)
+        ref64, _ = o.fmm64(cost, seeds)
+        out["cpu_fim_ms"], out["cpu_fmm_ms"] = us_fim / 1e3, us_fmm / 1e3
+        out["fim_vs_fmm"] = rel_diff(fmm, fim)
+        out["fim_vs_fmm64"] = fmm64_errors(fim, ref64)
+        for n, f in fields_out.items():
+            out[f"n{n}"]["check"] = {"max_rel_vs_fim": rel_diff(f, fim), "max_rel_vs_fmm": rel_diff(f, fmm),
+                                     "vs_fmm64": fmm64_errors(f, ref64), "residual": o.residual(cost, f)}
+    return out
 
 
 def run_batched(args, world, rank, local) -> int:
@@ -658,30 +662,9 @@ def run_maze(args, world, rank, local) -> int:
     return 0
 
 
-def main() -> int:
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ghcm", choices=["ghcm", "reference"])
-    ap.add_argument("--block", type=int, default=BLOCK)
-    ap.add_argument("--n", type=int, default=N_JOBS)
-    ap.add_argument("--kernel", default="systolic", choices=["systolic", "fim"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-n-sweep", action="store_true", help="time only the headline n")
-    ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain comparison")
-    ap.add_argument("--workload", default="ring", choices=["ring", "batched", "maze"])
-    ap.add_argument("--no-autotune", action="store_true",
-                    help="batched workload: use --block and --n instead of the autotuner's choice")
-    args = ap.parse_args()
-    world, rank, local = dist_env()
-    if args.impl == "reference":
-        return run_reference(args, world, rank)
-    if args.workload == "batched":
-        return run_batched(args, world, rank, local)
-    if args.workload == "maze":
-        return run_maze(args, world, rank, local)
-
+def run_ring(args, world, rank, local) -> int:
+    """C2 as its own line: the 4096^2 seven-ring field with the plain device
+    schedule at --n (the configuration's other n beside it)."""
     import torch
 
     import ghcm_gb300 as g
@@ -699,7 +682,7 @@ def main() -> int:
             dist.barrier()
         torch.cuda.synchronize(dev)
 
-    speed, seeds = make_workload()
+    speed, seeds = make_workload("ring")
     h, w = speed.shape
     cells = h * w
     cfg = g.HcmConfig(block_size=args.block, max_jobs=args.n, fim_minimum_change=EPS,
@@ -795,7 +778,7 @@ def main() -> int:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "step_ms": step_spread, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "block": args.block, "n": args.n, "kernel": args.kernel, "eps": EPS,
+        "config": {"workload": RING_WORKLOAD, "block": args.block, "n": args.n, "kernel": args.kernel, "eps": EPS,
                    "sources": int(len(seeds)), "l2": "flushed between steps (256 MiB write outside the events)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * cells / (e2e_mean * 1e3), "unit": UNIT, "ms_per_step": e2e_mean,
@@ -829,9 +812,6 @@ def main() -> int:
             ref64, _ = Oracle().fmm64(cost, seeds)
             line["check"]["vs_fmm64"] = fmm64_errors(field, ref64)
             line["check"]["fim_vs_fmm64"] = fmm64_errors(fim, ref64)
-        if not args.no_learned:
-            line["learned_vs_plain"] = learned_vs_plain(g, dev, stream, flush, max(1, min(args.steps, 3)), 1,
-                                                        fp64=not args.no_cpu_baseline)
         if not args.no_cpu_baseline:
             line["small_ring_256"] = small_ring_check(g)
         print(json.dumps(line), flush=True)
@@ -839,6 +819,230 @@ def main() -> int:
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def run_noise(args, world, rank, local) -> int:
+    """The headline: the learned block schedule against the plain one on the
+    4096^2 noise field. `value` is the learned schedule's Mcell/s; the plain
+    schedule (n = PLAIN_N, the fastest plain n on this field) is timed the
+    same way in the same run beside it, with the other plain n and the veto
+    policy; both fields are checked against the reference FIM and FMM and the
+    FP64 FMM. The seven-ring field (C2) and the 256^2 ring (C1) ride along as
+    sub-objects."""
+    import torch
+
+    import ghcm_gb300 as g
+    from ghcm_gb300 import fields, learned
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    params, threshold, meta = learned.load_model(MODEL)
+    speed, seeds = make_workload("noise")
+    h, w = speed.shape
+    cells = h * w
+    d_speed = torch.from_numpy(speed).to(dev)
+    d_seeds = torch.from_numpy(seeds.astype(np.int32)).to(dev)
+    d_time_l = torch.empty_like(d_speed)
+    d_time_p = torch.empty_like(d_speed)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    s_learned = _learned_setup(g, learned, params, threshold, learned.POLICY_SCORE, **LEARNED_CAPS)
+    s_plain = g.HcmSetup(g.HcmConfig(block_size=BLOCK, max_jobs=PLAIN_N, fim_minimum_change=EPS))
+
+    for _ in range(args.warmup):
+        g.solve_device(s_learned, d_speed, d_seeds, d_time_l, stream=stream)
+        g.solve_device(s_plain, d_speed, d_seeds, d_time_p, stream=stream)
+    barrier()
+
+    def timed(setup, d_time):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        sts = []
+        barrier()
+        for i in range(args.steps):
+            flush.fill_(float(i))  # evict the fields from L2 between steps (outside the events)
+            ev[i][0].record(stream)
+            sts.append(g.solve_device(setup, d_speed, d_seeds, d_time, stream=stream))
+            ev[i][1].record(stream)
+        barrier()
+        return [a.elapsed_time(b) for a, b in ev], sts
+
+    with Clocks(local) as clk:
+        t_wall = time.perf_counter()
+        step_ms, stats = timed(s_learned, d_time_l)
+        t_wall = time.perf_counter() - t_wall
+        plain_ms, plain_stats = timed(s_plain, d_time_p)
+    clocks = clk.summary()
+    ms = sum(step_ms) / len(step_ms)
+    pms = sum(plain_ms) / len(plain_ms)
+    if dist is not None:
+        t = torch.tensor([ms, pms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, pms = float(t[0].item()), float(t[1].item())
+    value = world * cells / (ms * 1e3)
+    plain_value = world * cells / (pms * 1e3)
+    counters = learned.counters(s_learned)
+
+    # end to end through the public host-pointer call (pinned speed in, time field out), both schedules
+    h_speed = torch.from_numpy(speed).pin_memory()
+    h_time = torch.empty((h, w), dtype=torch.float32).pin_memory()
+
+    def e2e_of(setup):
+        g.eikonal_hcm_cuda_ex(setup, h_speed.numpy(), seeds, input_is_speed=True, out=h_time.numpy())  # warm-up
+        out = []
+        for _ in range(max(3, min(args.steps, 5))):
+            t0 = time.perf_counter()
+            g.eikonal_hcm_cuda_ex(setup, h_speed.numpy(), seeds, input_is_speed=True, out=h_time.numpy())
+            out.append((time.perf_counter() - t0) * 1e3)
+        return statistics.median(out), out
+
+    e2e_ms, e2e_samples = e2e_of(s_learned)
+    e2e_plain_ms = e2e_of(s_plain)[0] if not args.quick else float("nan")
+    if dist is not None:
+        t = torch.tensor([e2e_ms, e2e_plain_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms, e2e_plain_ms = float(t[0].item()), float(t[1].item())
+    # leave each schedule's device-resident field for the checks
+    g.solve_device(s_learned, d_speed, d_seeds, d_time_l, stream=stream)
+    g.solve_device(s_plain, d_speed, d_seeds, d_time_p, stream=stream)
+    field_l = d_time_l.cpu().numpy()
+    field_p = d_time_p.cpu().numpy()
+
+    # the plain schedule's other n and the veto policy, device-timed (fewer steps)
+    k = max(1, min(args.steps, 3))
+    others, other_fields = {}, {}
+    for n in PLAIN_SWEEP:
+        if n == PLAIN_N or args.quick:
+            continue
+        with g.HcmSetup(g.HcmConfig(block_size=BLOCK, max_jobs=n, fim_minimum_change=EPS)) as s:
+            d_t = torch.empty_like(d_speed)
+            o_ms, o_st = timed_device_solves(g, s, d_speed, d_seeds, d_t, stream, flush, k, 1)
+        other_fields[f"plain_n{n}"] = d_t.cpu().numpy()
+        others[f"plain_n{n}"] = {"mcells": cells / (o_ms * 1e3), "ms": o_ms,
+                                 "block_solves": statistics.mean(x["block_solves"] for x in o_st),
+                                 "waves": statistics.mean(x["waves"] for x in o_st)}
+    if not args.quick:
+        s_veto = _learned_setup(g, learned, params, threshold, learned.POLICY_VETO, max_jobs=PLAIN_N)
+        d_t = torch.empty_like(d_speed)
+        o_ms, o_st = timed_device_solves(g, s_veto, d_speed, d_seeds, d_t, stream, flush, k, 1)
+        other_fields["learned_veto_n1024"] = d_t.cpu().numpy()
+        others["learned_veto_n1024"] = {"mcells": cells / (o_ms * 1e3), "ms": o_ms,
+                                        "block_solves": statistics.mean(x["block_solves"] for x in o_st),
+                                        "waves": statistics.mean(x["waves"] for x in o_st)}
+        s_veto.close()
+
+    solves = statistics.mean(st["block_solves"] for st in stats)
+    plain_solves = statistics.mean(st["block_solves"] for st in plain_stats)
+    k_ms = statistics.mean(st["kernel_ms"] for st in stats)
+    bps = bytes_per_solve(BLOCK)
+    achieved = solves * bps / (k_ms * 1e-3) / 1e9
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms,
+        "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "schedule": "learned (score policy)", "block": BLOCK, **LEARNED_CAPS,
+                   "model": MODEL.name, "model_train_seeds": int(len(meta.get("train_seeds", []))),
+                   "threshold": threshold, "field_seed": NOISE_EVAL_SEED, "sources": int(len(seeds)), "eps": EPS,
+                   "l2": "flushed between steps (256 MiB write outside the events)",
+                   "parallelism": f"replicas x{world}"},
+        "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": pms, "n": PLAIN_N,
+                  "block_solves": plain_solves, "waves": statistics.mean(st["waves"] for st in plain_stats),
+                  "kernel_ms": statistics.mean(st["kernel_ms"] for st in plain_stats),
+                  "e2e": None if args.quick else {"value": world * cells / (e2e_plain_ms * 1e3), "unit": UNIT,
+                                                  "ms_per_step": e2e_plain_ms}},
+        "learned_vs_plain": {"mcells_ratio": value / plain_value, "block_solves_ratio": solves / plain_solves,
+                             "waves_ratio": statistics.mean(st["waves"] for st in stats) /
+                                            statistics.mean(st["waves"] for st in plain_stats)},
+        "e2e": {"value": world * cells / (e2e_ms * 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": cells * 4 + int(seeds.nbytes), "d2h_bytes_per_step": cells * 4,
+                "samples_ms": e2e_samples, "api": "ghcm_solve (host pointers, pinned)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": load_traffic("k_solve_noise4096_learned.json"),
+                     "kernel": f"k_solve<{BLOCK},systolic> (learned schedule)",
+                     "bytes_per_block_solve": bps, "block_solves": solves, "kernel_ms": k_ms,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in peaks else "fallback"},
+        "others": others,
+        "gpu_launches": LAUNCHES_PER_LEARNED_SOLVE * args.steps,
+        "clocks": clocks,
+        "solver": {"waves": statistics.mean(st["waves"] for st in stats),
+                   "residual_passes": statistics.mean(st["residual_passes"] for st in stats),
+                   "max_active": max(st["max_active"] for st in stats), "counters": counters,
+                   "wall_s_timed": t_wall},
+    }
+    if rank == 0:
+        from oracle.oracle import Oracle, rel_diff  # checker: parity of the benchmarked fields
+
+        cost = fields.cost_from_speed(speed)
+        o = Oracle()
+        line["check"] = {"residual": o.residual(cost, field_l), "residual_plain": o.residual(cost, field_p),
+                         "seeds_zero": bool(np.all(field_l[seeds[:, 1], seeds[:, 0]] == 0)),
+                         "learned_vs_plain_max_rel": rel_diff(field_l, field_p)}
+        if not args.no_cpu_baseline:
+            fim, fmm, base = cpu_baseline(speed, seeds)
+            line["cpu_baseline"] = base
+            ref64, _ = o.fmm64(cost, seeds)
+            line["check"].update({
+                "max_rel_vs_fim": rel_diff(field_l, fim), "max_rel_vs_fmm": rel_diff(field_l, fmm),
+                "plain_max_rel_vs_fim": rel_diff(field_p, fim), "plain_max_rel_vs_fmm": rel_diff(field_p, fmm),
+                "fim_vs_fmm": rel_diff(fim, fmm), "vs_fmm64": fmm64_errors(field_l, ref64),
+                "plain_vs_fmm64": fmm64_errors(field_p, ref64), "fim_vs_fmm64": fmm64_errors(fim, ref64)})
+            for name, f in other_fields.items():
+                others[name]["max_rel_vs_fim"] = rel_diff(f, fim)
+            if not args.quick:
+                line["reference_schedule_n1024"] = reference_schedule(o, cost, seeds, BLOCK, PLAIN_N, 256, fim)
+        if not args.quick:
+            line["ring_4096"] = ring_4096(g, dev, stream, flush, k, 1, checks=not args.no_cpu_baseline)
+        if not args.no_cpu_baseline and not args.quick:
+            line["small_ring_256"] = small_ring_check(g)
+        print(json.dumps(line), flush=True)
+    s_learned.close()
+    s_plain.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ghcm", choices=["ghcm", "reference"])
+    ap.add_argument("--block", type=int, default=BLOCK)
+    ap.add_argument("--n", type=int, default=N_JOBS)
+    ap.add_argument("--kernel", default="systolic", choices=["systolic", "fim"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-n-sweep", action="store_true", help="time only the headline n")
+    ap.add_argument("--quick", action="store_true",
+                    help="default workload: the headline pair only (no other n, veto policy or ring sub-objects)")
+    ap.add_argument("--workload", default="noise", choices=["noise", "ring", "batched", "maze"])
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batched workload: use --block and --n instead of the autotuner's choice")
+    args = ap.parse_args()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    if args.workload == "batched":
+        return run_batched(args, world, rank, local)
+    if args.workload == "maze":
+        return run_maze(args, world, rank, local)
+    if args.workload == "ring":
+        return run_ring(args, world, rank, local)
+    return run_noise(args, world, rank, local)
+
 
 
 if __name__ == "__main__":
