@@ -59,6 +59,7 @@ GHCM_MLP_FEATURES = 12
 GHCM_MLP_HIDDEN = 64
 GHCM_MLP_PARAMS = 5057
 GHCM_REFRESH_OFF = 0xFFFFFFFF
+GHCM_REFRESH_IN_SOLVE = 0xFFFFFFFE
 GHCM_POLICY_SCORE = 0
 GHCM_POLICY_VETO = 1
 

@@ -27,7 +27,9 @@ int check_config(const ghcm_config* c) {
         return GHCM_ERR_BAD_ARG;
     if (!(c->eps >= 0.f) || !std::isfinite(c->eps)) return GHCM_ERR_BAD_ARG;
     if (!(c->cost_cap >= 0.f)) return GHCM_ERR_BAD_ARG;  // NaN or negative
-    if (c->refresh_solves > kMaxRefresh && c->refresh_solves != GHCM_REFRESH_OFF) return GHCM_ERR_BAD_ARG;
+    if (c->refresh_solves > kMaxRefresh && c->refresh_solves != GHCM_REFRESH_OFF &&
+        c->refresh_solves != GHCM_REFRESH_IN_SOLVE)
+        return GHCM_ERR_BAD_ARG;
     for (uint32_t r : c->reserved)
         if (r != 0) return GHCM_ERR_BAD_ARG;
     return GHCM_OK;

@@ -142,8 +142,10 @@ inline void fill_sched_params(Sched& s, const ghcm_config& cfg, int sms, uint32_
     s.max_sweeps = cfg.max_sweeps ? cfg.max_sweeps : 4u * B * B;
     s.max_waves = cfg.max_waves;
     s.eps = cfg.eps;
-    s.refresh = cfg.refresh_solves == GHCM_REFRESH_OFF ? 0u
-                : (cfg.refresh_solves ? cfg.refresh_solves : kDefaultRefresh);
+    bool const off = cfg.refresh_solves == GHCM_REFRESH_OFF;
+    bool const in_only = cfg.refresh_solves == GHCM_REFRESH_IN_SOLVE;
+    s.refresh = static_cast<uint16_t>(off || in_only ? 0u : (cfg.refresh_solves ? cfg.refresh_solves : kDefaultRefresh));
+    s.in_solve = off ? 0u : 1u;
     s.learn.fallback_jobs = cfg.fallback_jobs ? cfg.fallback_jobs : s.max_jobs;
     s.timeout_ns = static_cast<uint64_t>(cfg.wait_timeout_ms ? cfg.wait_timeout_ms : 2000u) * 1000000ull;
 }

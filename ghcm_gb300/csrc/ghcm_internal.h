@@ -31,7 +31,7 @@ enum : uint32_t {
     kSolveMask = 0xFu << 8,
 };
 constexpr uint32_t kMaxRefresh = 15;  // largest Sched::refresh the 4-bit solve count holds
-constexpr uint32_t kDefaultRefresh = 8;
+constexpr uint32_t kDefaultRefresh = 1;
 
 __host__ __device__ __forceinline__ uint32_t solve_count(uint32_t flags) { return (flags & kSolveMask) >> 8; }
 
@@ -137,8 +137,8 @@ struct Sched {
     uint32_t  max_sweeps;
     uint32_t  max_waves;
     float     eps;
-    uint32_t  refresh;             // block-solves per tile that recompute every cell from its neighbours
-                                   // (cells may rise); later solves of the tile only lower cells
+    uint16_t  refresh;             // quiet block-solves per tile that may raise cells (kUpdFresh)
+    uint16_t  in_solve;            // 1: the other solves recompute cells up to their staged value (kUpdInSolve)
     uint64_t  timeout_ns;
     Learn     learn;
 };

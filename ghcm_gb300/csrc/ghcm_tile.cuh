@@ -187,16 +187,19 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         v[k] = inside[k] && c[k] < f_inf() && t[k] != 0.f;  // a time of 0 is a seed: fixed
     }
     float const eps = s.eps;
-    // Until the tile has had `refresh` quiet block-solves (solves that moved
-    // no cell far, falls_far), every solve recomputes each cell from its
-    // neighbours, so a cell may rise; after that, and past fresh_sweeps sweeps
-    // within a solve, cells only fall. Rounding makes the update slightly
-    // non-monotone: keeping the minimum of every evaluation (the reference's
-    // form) leaves a cell an ulp low here and there, and along a long front
-    // those ulps add up. Recomputing removes that drift; the budget ends the
-    // one-ulp oscillations of nearly tied neighbours, which only quiet
-    // solves make.
-    bool fresh = solve_count(flags) < s.refresh;
+    // Rounding makes the update slightly non-monotone, so keeping the minimum
+    // of every evaluation (the reference's min(T_old, update)) leaves a cell
+    // an ulp low wherever one evaluation rounded low, and along a long front
+    // those ulps add up; a block-solve evaluates each cell ~B times. So the
+    // sweeps recompute each cell from its neighbours, bounded by the cell's
+    // value when this solve began (kUpdInSolve: nothing rises above what
+    // neighbours saw). Until the tile has had `refresh` quiet block-solves
+    // (solves that moved no cell far, falls_far) the bound is dropped
+    // (kUpdFresh: a value an earlier solve rounded low rises again and the
+    // neighbours are told). Past fresh_sweeps sweeps, and for the reference
+    // form, cells only fall (kUpdKeepMin); the limits end the one-ulp
+    // oscillations of nearly tied neighbours.
+    int mode = solve_count(flags) < s.refresh ? kUpdFresh : (s.in_solve ? kUpdInSolve : kUpdKeepMin);
     uint32_t const fresh_sweeps = 4u * B;
     bool own_changed = false;
     bool capped = false;
@@ -211,9 +214,9 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
                 int const i = idx[k];
                 float const ax = fminf(sm.time[i - 1], sm.time[i + 1]);
                 float const ay = fminf(sm.time[i - BW], sm.time[i + BW]);
-                float const nt = next_time(godunov2_raw(ax, ay, c[k], c2[k]), t[k], fresh);
+                float const nt = next_time(godunov2_raw(ax, ay, c[k], c2[k]), t[k], t0[k], mode);
                 if (nt != t[k]) {
-                    moved |= moves(nt, t[k], eps, fresh);
+                    moved |= moves(nt, t[k], eps, mode != kUpdKeepMin);
                     t[k] = nt;
                     sm.time[i] = nt;
                     own_changed = true;
@@ -221,7 +224,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
             }
             ++sweeps;
             if (!__syncthreads_or(moved)) break;
-            if (sweeps >= fresh_sweeps) fresh = false;
+            if (sweeps >= fresh_sweeps) mode = kUpdKeepMin;
             if (sweeps >= s.max_sweeps) {
                 capped = true;
                 break;
@@ -252,10 +255,10 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
                     int const i = idx[k];
                     float const ax = fminf(sm.time[i - 1], sm.time[i + 1]);
                     float const ay = fminf(sm.time[i - BW], sm.time[i + BW]);
-                    float const nt = next_time(godunov2_raw(ax, ay, c[k], c2[k]), t[k], fresh);
+                    float const nt = next_time(godunov2_raw(ax, ay, c[k], c2[k]), t[k], t0[k], mode);
                     bool moved = false;
                     if (nt != t[k]) {
-                        moved = moves(nt, t[k], eps, fresh);
+                        moved = moves(nt, t[k], eps, mode != kUpdKeepMin);
                         t[k] = nt;
                         sm.time[i] = nt;
                         own_changed = true;
@@ -280,9 +283,9 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
                             int const i = idx[k];
                             float const ax = fminf(sm.time[i - 1], sm.time[i + 1]);
                             float const ay = fminf(sm.time[i - BW], sm.time[i + BW]);
-                            float const nt = next_time(godunov2_raw(ax, ay, c[k], c2[k]), t[k], fresh);
+                            float const nt = next_time(godunov2_raw(ax, ay, c[k], c2[k]), t[k], t0[k], mode);
                             if (nt != t[k]) {
-                                open[k] = moves(nt, t[k], eps, fresh);
+                                open[k] = moves(nt, t[k], eps, mode != kUpdKeepMin);
                                 t[k] = nt;
                                 sm.time[i] = nt;
                                 own_changed = true;
@@ -293,7 +296,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
                 }
                 ++sweeps;
                 if (!__syncthreads_or(still_open)) break;
-                if (sweeps >= fresh_sweeps) fresh = false;
+                if (sweeps >= fresh_sweeps) mode = kUpdKeepMin;
                 if (sweeps >= s.max_sweeps) {
                     capped = true;
                     break;
@@ -345,7 +348,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
                 float const a_lat = (e & 1) ? fminf(sm.time[pi - 1], sm.time[pi + 1])
                                             : fminf(sm.time[pi - BW], sm.time[pi + BW]);
                 bool const track_rise = s.refresh != 0u;
-                float const nt = next_time(godunov_raw(a_norm, a_lat, cp), told, track_rise);
+                float const nt = next_time(godunov_raw(a_norm, a_lat, cp), told, told, track_rise ? kUpdFresh : kUpdKeepMin);
                 if (moves(nt, told, eps, track_rise)) {
                     e_imp = true;
                     e_key = nt;
@@ -443,7 +446,7 @@ __device__ void residual_warp(const Sched& s, uint32_t nxt, uint32_t warp_global
             float const xr = gx + 1 < static_cast<int>(I.w) ? __ldcg(&I.time[gi + 1]) : f_inf();
             float const yu = gy > 0 ? __ldcg(&I.time[gi - I.w]) : f_inf();
             float const yd = gy + 1 < static_cast<int>(I.h) ? __ldcg(&I.time[gi + I.w]) : f_inf();
-            float const nt = next_time(godunov_raw(fminf(xl, xr), fminf(yu, yd), cst), t, fresh);
+            float const nt = next_time(godunov_raw(fminf(xl, xr), fminf(yu, yd), cst), t, t, fresh ? kUpdFresh : kUpdKeepMin);
             if (moves(nt, t, s.eps, fresh)) {
                 bad = true;
                 kmin = fminf(kmin, fminf(nt, t));

@@ -108,12 +108,13 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     }
     __syncwarp();
 
-    float t[R], c[R], c2[R];
+    float t[R], t0[R], c[R], c2[R];
     bool fix[R];  // seeds (time 0) and walls keep their value
 #pragma unroll
     for (int k = 0; k < R; ++k) {
         int const i = si<B>(x, band * R + k);
         t[k] = sm.time[i];
+        t0[k] = t[k];
         c[k] = sm.cost[i];
         c2[k] = __fmul_rn(__fmul_rn(c[k], c[k]), 2.0f);
         fix[k] = t[k] == 0.f || !(c[k] < f_inf());
@@ -121,8 +122,8 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     float const h_top = sm.time[si<B>(x, -1)];  // used by band 0
     float const h_bot = sm.time[si<B>(x, B)];   // used by the last band
     float const eps = s.eps;
-    // until the tile has had `refresh` quiet block-solves it recomputes its cells (see solve_tile)
-    bool fresh = solve_count(sm.claim[0]) < s.refresh;
+    // how sweeps bound the update (see solve_tile)
+    int mode = solve_count(sm.claim[0]) < s.refresh ? kUpdFresh : (s.in_solve ? kUpdInSolve : kUpdKeepMin);
     uint32_t const fresh_sweeps = 4u * B;
     bool changed = false;
     bool capped = false;
@@ -140,8 +141,8 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
             if (x == B - 1) r = sm.time[si<B>(B, band * R + k)];
             float const u = (k > 0) ? t[k > 0 ? k - 1 : 0] : (band > 0 ? up_in : h_top);
             float const d = (k < R - 1) ? t[k < R - 1 ? k + 1 : 0] : (band < W::G - 1 ? down_in : h_bot);
-            nt[k] = fix[k] ? t[k] : next_time(godunov2_raw(fminf(l, r), fminf(u, d), c[k], c2[k]), t[k], fresh);
-            moved |= moves(nt[k], t[k], eps, fresh);
+            nt[k] = fix[k] ? t[k] : next_time(godunov2_raw(fminf(l, r), fminf(u, d), c[k], c2[k]), t[k], t0[k], mode);
+            moved |= moves(nt[k], t[k], eps, mode != kUpdKeepMin);
         }
 #pragma unroll
         for (int k = 0; k < R; ++k) {
@@ -150,7 +151,7 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
         }
         ++sweeps;
         if (!__any_sync(FULL, moved)) break;
-        if (sweeps >= fresh_sweeps) fresh = false;
+        if (sweeps >= fresh_sweeps) mode = kUpdKeepMin;
         if (sweeps >= s.max_sweeps) {
             capped = true;
             break;
@@ -204,7 +205,7 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
                 float const a_lat = (e & 1) ? fminf(sm.time[pi - 1], sm.time[pi + 1])
                                             : fminf(sm.time[pi - G::BW], sm.time[pi + G::BW]);
                 bool const track_rise = s.refresh != 0u;
-                float const nv = next_time(godunov_raw(a_norm, a_lat, cp), told, track_rise);
+                float const nv = next_time(godunov_raw(a_norm, a_lat, cp), told, told, track_rise ? kUpdFresh : kUpdKeepMin);
                 if (moves(nv, told, eps, track_rise)) {
                     imp = true;
                     key = nv;

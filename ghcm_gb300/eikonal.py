@@ -69,7 +69,7 @@ class HcmConfig:
     device: int = -1
     fallback_jobs: int = 0                 # learned schedule: n of a wave in which no tile qualifies
     cost_cap: float = 0.0                  # > 0: cost = min(cost, cost_cap) (field_cost_as_permeable)
-    refresh_solves: int = 0                # solves per tile that recompute cells (0 = 8; _lib.GHCM_REFRESH_OFF = none)
+    refresh_solves: int = 0                # quiet solves per tile that may raise cells (0 = 1; _lib.GHCM_REFRESH_*)
 
     def to_c(self, sm_count: int | None = None) -> GhcmConfig:
         c = GhcmConfig()

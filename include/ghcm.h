@@ -50,9 +50,12 @@ extern "C" {
 #define GHCM_SCHEDULE_PLAIN   0    /* lowest-key-first top-n (the reference's priority queue) */
 #define GHCM_SCHEDULE_LEARNED 1    /* learned block-scheduling score */
 
-/* ghcm_config.refresh_solves: no block-solve recomputes cells; every update keeps
- * min(T_old, update) */
-#define GHCM_REFRESH_OFF 0xFFFFFFFFu
+/* ghcm_config.refresh_solves, special values:
+ *   GHCM_REFRESH_OFF      the reference's form everywhere: every update keeps min(T_old, update)
+ *   GHCM_REFRESH_IN_SOLVE sweeps recompute cells up to their value at the start of the block-solve;
+ *                         no block-solve raises a cell */
+#define GHCM_REFRESH_OFF      0xFFFFFFFFu
+#define GHCM_REFRESH_IN_SOLVE 0xFFFFFFFEu
 
 /* ghcm_config.key_mode - the plain priority key */
 #define GHCM_KEY_BOUNDARY_MIN 0    /* min arrival time among the boundary values that activated the tile */
@@ -77,11 +80,13 @@ typedef struct ghcm_config {
     float    cost_cap;        /* > 0: cost = min(cost, cost_cap), the reference's permeable-wall
                                  transform field_cost_as_permeable (src/test_runner.cpp:70-75,
                                  default there 1e3); 0 = no cap */
-    uint32_t refresh_solves;  /* block-solves of each tile that recompute every cell from its
-                                 neighbours, so a cell may rise; the tile's later solves only lower
-                                 cells, as the reference's min(T_old, update) does
-                                 (data/eikonal_common.cl:288-308). 0 = 8; 1..15; GHCM_REFRESH_OFF =
-                                 none (every update keeps the minimum) */
+    uint32_t refresh_solves;  /* rounding makes the update slightly non-monotone, and keeping
+                                 min(T_old, update) of every evaluation (data/eikonal_common.cl:
+                                 288-308) lets ulps drift low along a front. Sweeps therefore
+                                 recompute each cell, bounded by its value at the start of the
+                                 block-solve; the first refresh_solves quiet block-solves of a tile
+                                 drop that bound (cells may rise, neighbours are told).
+                                 0 = the default (1); 1..15; GHCM_REFRESH_IN_SOLVE; GHCM_REFRESH_OFF */
     uint32_t reserved[2];     /* must be zero */
 } ghcm_config;
 

@@ -85,7 +85,7 @@ struct HcmConfig {
     uint32_t max_waves = 0;
     uint32_t wait_timeout_ms = 2000;
     bool use_tma = true;
-    uint32_t refresh_solves = 0;          // solves per tile that recompute cells (0 = 8, GHCM_REFRESH_OFF = none)
+    uint32_t refresh_solves = 0;          // quiet solves per tile that may raise cells (0 = 1, GHCM_REFRESH_*)
 };
 
 struct EikonalResult {

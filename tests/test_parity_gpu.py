@@ -297,3 +297,17 @@ def test_permeable_cost_cap(setups, oracle_lib, block):
     # the cost form of the input gives the same field
     res2 = g.eikonal_hcm_cuda_ex(setups(block, cost_cap=1e3), fields.cost_from_speed(speed), seeds)
     check_field(res2.field, ref, seeds)
+
+
+@pytest.mark.parametrize("refresh", [_lib.GHCM_REFRESH_OFF, _lib.GHCM_REFRESH_IN_SOLVE, 1, 4, 15])
+@pytest.mark.parametrize("block,kernel", [(8, g.Kernel.Systolic), (16, g.Kernel.Systolic), (16, g.Kernel.FIM),
+                                          (32, g.Kernel.Systolic)])
+def test_update_bounds_keep_parity(setups, medium, refresh, block, kernel):
+    """Every way a sweep may bound the update (the reference's min(T_old, .),
+    recompute up to the staged value, and 1-15 quiet solves that may raise
+    cells) converges to the oracle's field within the bar on the medium cases."""
+    for case in ("ring7_1024", "noise_1024"):
+        speed, cost, seeds, ref = medium[case]
+        res = g.eikonal_hcm_cuda_ex(setups(block, kernel, max_jobs=1024, refresh_solves=refresh), speed, seeds,
+                                    input_is_speed=True)
+        check_field(res.field, ref, seeds)
