@@ -45,7 +45,8 @@ static_assert(kParams == GHCM_MLP_PARAMS && kFeatures == GHCM_MLP_FEATURES && kH
               "MLP shape differs from the C ABI");
 static_assert(sizeof(TraceRec) == sizeof(ghcm_trace_record), "trace record layout differs from the C ABI");
 
-// Bytes of the per-tile learning arrays (tstat | kmax | nsolve | last_change | vetoes | score | score_tag).
+// Bytes of the per-tile learning arrays (tstat | kmax | nsolve | last_change | vetoes | the scores of the
+// entries of the two active lists).
 inline size_t learn_bytes(uint32_t tiles) {
     return align_up(16ull * tiles, 256) + 6 * align_up(4ull * tiles, 256);
 }
@@ -58,8 +59,8 @@ inline void bind_learn_arrays(Learn& L, char* base, uint32_t tiles) {
     L.nsolve = reinterpret_cast<uint32_t*>(base + a + b);
     L.last_change = reinterpret_cast<uint32_t*>(base + a + 2 * b);
     L.vetoes = reinterpret_cast<uint32_t*>(base + a + 3 * b);
-    L.score = reinterpret_cast<float*>(base + a + 4 * b);
-    L.score_tag = reinterpret_cast<uint32_t*>(base + a + 5 * b);
+    L.lscore[0] = reinterpret_cast<float*>(base + a + 4 * b);
+    L.lscore[1] = reinterpret_cast<float*>(base + a + 5 * b);
 }
 
 inline int map_cuda(cudaError_t e) {

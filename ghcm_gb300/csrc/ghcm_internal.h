@@ -105,8 +105,8 @@ struct Learn {
     uint32_t* nsolve;      // per tile: block-solves so far
     uint32_t* last_change; // per tile: wave of its last useful solve + 1 (0: none)
     uint32_t* vetoes;      // per tile: consecutive vetoes (veto mode)
-    float*    score;       // per tile: model logit, written by the solve that queued it (score mode)
-    uint32_t* score_tag;   // per tile: 1 while score[] belongs to the tile's current activation
+    float*    lscore[2];   // per entry of active list L: the tile's model logit (score mode), written by the
+                           // solve that queued it; +inf for tiles re-queued in full, -inf until scored
     const float* params;   // MLP parameters (kParams floats); nullptr: plain schedule
     TraceRec* trace;       // trace records; nullptr: no trace
     uint32_t  trace_cap;

@@ -135,24 +135,20 @@ __device__ void tile_speed_stats(const Sched& s, uint32_t tile) {
     }
 }
 
-// Score policy: the model logit of `tile`, just queued for the next wave by
-// the calling CTA's solve, computed by the calling warp and kept in score[]
-// (score_tag = 1) for the next decision. Tiles re-queued in full need none
-// (they are always taken). A tile queued by two neighbours is scored twice;
-// the later write stands.
-__device__ void score_queued_warp(const Sched& s, uint32_t tile, uint32_t wave) {
+// Score policy: the model logit of `tile`, just appended at entry `pos` of
+// list[nxt] by the calling CTA's solve, computed by the calling warp and kept
+// in that entry's score for the next decision. Tiles re-queued in full need
+// none (they are always taken).
+__device__ void score_queued_warp(const Sched& s, uint32_t tile, uint32_t nxt, uint32_t pos, uint32_t wave) {
     uint32_t const flags = ld_relaxed(&s.flags[tile]);
-    if (!(flags & kActive) || (flags & kFull)) return;
+    if (flags & kFull) return;
     Ctl* ctl = s.ctl;
     float const key = __uint_as_float(__ldcg(&s.key[tile]));
     float const kmax = __uint_as_float(__ldcg(&s.learn.kmax[tile]));
     float x[kFeatures];
     tile_features(s, tile, flags, key, kmax, wave, ld_relaxed_f(&ctl->wave_front), ld_relaxed_f(&ctl->wave_span), x);
     float const z = mlp_logit_warp(g_mlp_params, x);
-    if ((threadIdx.x & 31) == 0) {
-        __stcg(&s.learn.score[tile], z);
-        __stcg(&s.learn.score_tag[tile], 1u);
-    }
+    if ((threadIdx.x & 31) == 0) __stcg(&s.learn.lscore[nxt][pos], z);
 }
 
 }  // namespace ghcm
@@ -166,7 +162,6 @@ __device__ __forceinline__ uint32_t learn_claim(const Sched& s, uint32_t tile, u
                                                 uint32_t wave, float* feat) {
     if (!s.learn.tstat) return 0u;
     uint32_t const kmx = atomicExch(&s.learn.kmax[tile], 0u);
-    if (s.learn.score_tag) __stcg(&s.learn.score_tag[tile], 0u);  // its score belonged to this activation
     if (s.learn.trace) {
         float f[kFeatures];
         tile_features(s, tile, flags, __uint_as_float(key_bits), __uint_as_float(kmx), wave,

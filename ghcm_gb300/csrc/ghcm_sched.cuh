@@ -67,14 +67,17 @@ __device__ __forceinline__ float to_cost(const Inst& I, float v) {
     return cap_cost(I, I.in_is_speed ? __fdiv_rn(I.spacing, v) : v);
 }
 
+constexpr uint32_t kNoPos = 0xffffffffu;
+
 // Puts `tile` into the next active set: lowers its key to `key`, ORs `bits`
 // into its flags and appends it to list[nxt] unless it is already active.
 // The device form of the dirty-set test + heap push + border-mask OR of
 // src/eikonal_hcm.cpp:451-462. s_krange (the calling CTA's {min, max} key
-// bits of what it activated this phase) is widened to `key`. Returns true
-// when this call appended the tile (it was idle).
-__device__ __forceinline__ bool activate(const Sched& s, uint32_t tile, uint32_t bits, float key, uint32_t nxt,
-                                         uint32_t* s_krange) {
+// bits of what it activated this phase) is widened to `key`. Returns the
+// tile's position in list[nxt] when this call appended it (it was idle),
+// else kNoPos.
+__device__ __forceinline__ uint32_t activate(const Sched& s, uint32_t tile, uint32_t bits, float key, uint32_t nxt,
+                                             uint32_t* s_krange) {
     uint32_t const kb = __float_as_uint(key);
     atomicMin(&s.key[tile], kb);
     if (s.learn.kmax) atomicMax(&s.learn.kmax[tile], kb);
@@ -85,16 +88,21 @@ __device__ __forceinline__ bool activate(const Sched& s, uint32_t tile, uint32_t
     uint32_t const old = atom_or_release(&s.flags[tile], kActive | bits);
     if (!(old & kActive)) {
         uint32_t const pos = atomicAdd(&s.ctl->count[nxt], 1u);
-        if (pos < s.num_tiles)
+        if (pos < s.num_tiles) {
             s.list[nxt][pos] = tile;
-        else
-            atomicOr(&s.ctl->error, kErrInternal);
-        return true;
+            // learned score policy: tiles re-queued in full always go; others wait for a score
+            if (s.learn.lscore[nxt]) s.learn.lscore[nxt][pos] = (bits & kFull) ? f_inf() : -f_inf();
+            return pos;
+        }
+        atomicOr(&s.ctl->error, kErrInternal);
     }
-    return false;
+    return kNoPos;
 }
 
 // Priority key of an active tile (smaller = solved first), as float bits.
+// Keys stay exact: a tile activated again with a lower key moves up (the
+// reference freezes a heap entry's key, src/eikonal_hcm.cpp:74-75, and on the
+// 4096^2 rings frozen keys took the device schedule from 766 to 2,338 waves).
 __device__ __forceinline__ uint32_t tile_key(const Sched& s, uint32_t tile) {
     if (s.key_mode == 0u) return __ldcg(&s.key[tile]);
     // Block-min key: smallest_time of the tile and of its 4 neighbours
@@ -119,12 +127,15 @@ __device__ __forceinline__ uint32_t tile_key(const Sched& s, uint32_t tile) {
 constexpr int SELECT_BINS = 2048;
 
 template <int THREADS, int CACHE>
-__device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t m, uint32_t n, uint32_t* carry,
-                                 uint32_t* s_hist, uint32_t* s_sel, float lo, float hi, bool have_range,
-                                 uint32_t jobs_base) {
+__device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_t n, uint32_t* s_hist, uint32_t* s_sel,
+                                 float lo, float hi, bool have_range, uint32_t jobs_base) {
     __shared__ float s_fmin[THREADS / 32], s_fmax[THREADS / 32];
     int const tid = threadIdx.x;
     int const lane = tid & 31, warp = tid >> 5;
+    const uint32_t* list = s.list[L];
+    uint32_t* carry = s.list[L ^ 1u];
+    const float* score = s.learn.lscore[L];
+    float* carry_score = s.learn.lscore[L ^ 1u];
     for (int i = tid; i < SELECT_BINS; i += THREADS) s_hist[i] = 0u;
     if (!have_range) {
         // pass 1: range of the finite keys
@@ -164,8 +175,8 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
         return b < 0 ? 0 : (b >= SELECT_BINS ? SELECT_BINS - 1 : b);
     };
     // pass 2: histogram. Up to CACHE entries per thread (a register budget set
-    // by the kernel) keep their key in registers for the gather pass (lists of
-    // up to THREADS * CACHE tiles), so it re-reads only the coalesced list;
+    // by the kernel) keep their key in registers for the gather pass (lists
+    // of up to THREADS * CACHE tiles), so it re-reads only the coalesced list;
     // longer lists load keys again there.
     bool const cached = m <= static_cast<uint32_t>(THREADS * CACHE);
     uint32_t ck[CACHE];
@@ -177,10 +188,8 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
             ct[u] = (i < m) ? __ldcg(&list[i]) : 0u;
         }
 #pragma unroll
-        for (int u = 0; u < CACHE; ++u) {
-            uint32_t const i = tid + u * THREADS;
-            ck[u] = (i < m) ? tile_key(s, ct[u]) : 0u;
-        }
+        for (int u = 0; u < CACHE; ++u)
+            ck[u] = (tid + u * THREADS < m) ? tile_key(s, ct[u]) : 0u;
 #pragma unroll
         for (int u = 0; u < CACHE; ++u)
             if (tid + u * THREADS < m) atomicAdd(&s_hist[bin_of(__uint_as_float(ck[u]))], 1u);
@@ -236,8 +245,8 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
     __syncthreads();
     int const bnd = static_cast<int>(s_sel[0]);
     uint32_t const take_eq = s_sel[1];
-    // pass 3: gather
-    auto place = [&](uint32_t t, uint32_t kb) {
+    // pass 3: gather; a carried entry keeps its learned score
+    auto place = [&](uint32_t i, uint32_t t, uint32_t kb) {
         int const b = bin_of(__uint_as_float(kb));
         bool take = b < bnd;
         if (!take && b == bnd) take = atomicAdd(&s_sel[2], 1u) < take_eq;
@@ -246,14 +255,17 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
             if (GHCM_CHECK(s.ctl, pos < s.max_jobs, 9u)) s.jobs[pos] = t;
         } else {
             uint32_t const pos = atomicAdd(&s_sel[4], 1u);
-            if (GHCM_CHECK(s.ctl, pos < s.num_tiles, 10u)) carry[pos] = t;
+            if (GHCM_CHECK(s.ctl, pos < s.num_tiles, 10u)) {
+                carry[pos] = t;
+                if (score) carry_score[pos] = __ldcg(&score[i]);
+            }
         }
     };
     if (cached) {
 #pragma unroll
         for (int u = 0; u < CACHE; ++u) {
             uint32_t const i = tid + u * THREADS;
-            if (i < m) place(__ldcg(&list[i]), ck[u]);
+            if (i < m) place(i, __ldcg(&list[i]), ck[u]);
         }
     } else {
         uint32_t i = tid;
@@ -264,11 +276,11 @@ __device__ uint32_t select_top_n(const Sched& s, const uint32_t* list, uint32_t 
 #pragma unroll
             for (int u = 0; u < 4; ++u) k4[u] = tile_key(s, t4[u]);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) place(t4[u], k4[u]);
+            for (int u = 0; u < 4; ++u) place(i + u * THREADS, t4[u], k4[u]);
         }
         for (; i < m; i += THREADS) {
             uint32_t const t = __ldcg(&list[i]);
-            place(t, tile_key(s, t));
+            place(i, t, tile_key(s, t));
         }
     }
     __syncthreads();
@@ -324,8 +336,7 @@ __device__ void plan_plain_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t
     bool const all = m <= n;
     uint32_t carried = 0u;
     if (!all) {
-        carried = select_top_n<THREADS, CACHE>(s, s.list[L], m, n, s.list[L ^ 1u], s_hist, s_sel, lo, hi, s.key_mode == 0u,
-                                        base);
+        carried = select_top_n<THREADS, CACHE>(s, L, m, n, s_hist, s_sel, lo, hi, s.key_mode == 0u, base);
     } else if (base) {
         for (uint32_t i = threadIdx.x; i < m; i += THREADS) s.jobs[base + i] = __ldcg(&s.list[L][i]);
     }
@@ -340,8 +351,9 @@ __device__ void plan_plain_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t
 }
 
 // Learned schedule, score policy: the tiles of list[act] (m) re-queued in full
-// or whose score (written when they were queued) reaches the threshold become
-// jobs (at most max_jobs), the rest are carried to list[act ^ 1]; if fewer
+// or whose score (written at their list entry when they were queued) reaches
+// the threshold become jobs (at most max_jobs), the rest are carried to
+// list[act ^ 1]; if fewer
 // than fallback_jobs were taken the wave is filled from the carried tiles in
 // plain key order. Returns the list the JOBS phase treats as current (its
 // activations go to the other one). Counters and s_sel[8], [11] as in
@@ -358,7 +370,11 @@ __device__ uint32_t plan_learned_jobs(const Sched& s, uint32_t act, uint32_t m, 
         s_sel[7] = 0u;  // carried
     }
     __syncthreads();
-    auto place = [&](uint32_t t, bool take) {
+    const uint32_t* list = s.list[act];
+    const float* score = s.learn.lscore[act];
+    // a carried entry keeps its score
+    auto place = [&](uint32_t i, uint32_t t, float z) {
+        bool take = z >= thr;  // +inf for tiles re-queued in full
         if (take) {
             uint32_t const pos = atomicAdd(&s_sel[6], 1u);
             if (pos < cap)
@@ -366,28 +382,26 @@ __device__ uint32_t plan_learned_jobs(const Sched& s, uint32_t act, uint32_t m, 
             else
                 take = false;
         }
-        if (!take) s.list[act ^ 1u][atomicAdd(&s_sel[7], 1u)] = t;
+        if (!take) {
+            uint32_t const pos = atomicAdd(&s_sel[7], 1u);
+            s.list[act ^ 1u][pos] = t;
+            s.learn.lscore[act ^ 1u][pos] = z;
+        }
     };
+    // ids and scores are coalesced loads of the list
     uint32_t i = tid;
     for (; i + 3u * THREADS < m; i += 4u * THREADS) {  // four entries in flight per thread
-        uint32_t t4[4], f4[4], g4[4];
+        uint32_t t4[4];
         float z4[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) t4[u] = __ldcg(&s.list[act][i + u * THREADS]);
-#pragma unroll
         for (int u = 0; u < 4; ++u) {
-            f4[u] = ld_relaxed(&s.flags[t4[u]]);
-            g4[u] = __ldcg(&s.learn.score_tag[t4[u]]);
-            z4[u] = __ldcg(&s.learn.score[t4[u]]);
+            t4[u] = __ldcg(&list[i + u * THREADS]);
+            z4[u] = __ldcg(&score[i + u * THREADS]);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) place(t4[u], (f4[u] & kFull) || (g4[u] != 0u && z4[u] >= thr));
+        for (int u = 0; u < 4; ++u) place(i + u * THREADS, t4[u], z4[u]);
     }
-    for (; i < m; i += THREADS) {
-        uint32_t const t = __ldcg(&s.list[act][i]);
-        place(t, (ld_relaxed(&s.flags[t]) & kFull) ||
-                     (__ldcg(&s.learn.score_tag[t]) != 0u && __ldcg(&s.learn.score[t]) >= thr));
-    }
+    for (; i < m; i += THREADS) place(i, __ldcg(&list[i]), __ldcg(&score[i]));
     __syncthreads();
     uint32_t const take = min(s_sel[6], cap);
     uint32_t const carried = s_sel[7];

@@ -264,7 +264,6 @@ __global__ void k_init_inst(Sched s) {
             s.learn.nsolve[g] = 0u;
             s.learn.last_change[g] = 0u;
             s.learn.vetoes[g] = 0u;
-            s.learn.score_tag[g] = 0u;
         }
     }
     size_t const n = static_cast<size_t>(I.w) * I.h;

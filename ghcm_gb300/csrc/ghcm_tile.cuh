@@ -54,6 +54,7 @@ struct alignas(128) TileSmem {
     uint8_t check[B * B];  // block-FIM: re-check requests
     float feat[kFeatures]; // trace recorder: features of the current solve
     uint32_t queued[4];    // learned score policy: neighbour queued across edge e, or kNone
+    uint32_t queued_pos[4];  // and its entry in the next active list
 };
 
 constexpr uint32_t kNone = 0xffffffffu;
@@ -396,13 +397,16 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     uint32_t const edge_changed = s_word[4];
     if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u) &&
         GHCM_CHECK(s.ctl, nb >= 0 && static_cast<uint32_t>(nb) < s.num_tiles, 7u)) {
-        if (activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt, s_krange))
-            sm.queued[e] = static_cast<uint32_t>(nb);  // appended now: score it (a re-activation keeps its score)
+        uint32_t const pos = activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt, s_krange);
+        if (pos != kNoPos) {  // appended now: score it (a re-activation keeps its entry's score)
+            sm.queued[e] = static_cast<uint32_t>(nb);
+            sm.queued_pos[e] = pos;
+        }
     }
     if (s.learn.params && !s.learn.veto) {  // score policy: score what this solve queued, a warp per tile
         __syncthreads();
         for (int q = tid >> 5; q < 4; q += G::THREADS / 32)
-            if (sm.queued[q] != kNone) score_queued_warp(s, sm.queued[q], wave + 1u);
+            if (sm.queued[q] != kNone) score_queued_warp(s, sm.queued[q], nxt, sm.queued_pos[q], wave + 1u);
     }
 #ifdef GHCM_PROFILE
     if (tid == 0) {
