@@ -200,6 +200,14 @@ def load_traffic(name: str = "k_solve_ring7_4096.json", block: int | None = None
     return None
 
 
+def load_block_solves(name: str):
+    """Block-solves of the launch a committed capture summary covers, or None."""
+    try:
+        return json.loads((ROOT / "profiles" / name).read_text()).get("block_solves")
+    except (ValueError, OSError):
+        return None
+
+
 def batch_traffic(block: int, block_solves: float):
     """DRAM bytes of one batch launch: the captured bytes per block-solve
     (profiles/k_solve_batch512.json, same tile size) scaled to this run's
@@ -406,6 +414,36 @@ def ring_4096(g, dev, stream, flush, steps: int, warmup: int, checks: bool) -> d
     return out
 
 
+def kernel_compare(g, dev, stream, flush, steps: int) -> dict:
+    """The two tile kernels of the reference (systolic, data/eikonal_ghcm_systolic.cl,
+    and block-FIM, data/eikonal_ghcm_fim.cl:214-392) timed on the same fields:
+    the 256^2 ring (B = 8, n = 64), the 4096^2 rings (B = 16, n = 256) and the
+    4096^2 noise field (B = 16, n = 1024), plain schedule, device-resident."""
+    import torch
+
+    from ghcm_gb300 import fields
+
+    cases = {"ring7_256x256_b8_n64": (fields.ring7_small(seed=1), 8, 64),
+             "ring7_4096x4096_b16_n256": (fields.ring7_large(seed=1), 16, 256),
+             "noise_4096x4096_b16_n1024": (make_workload("noise"), 16, 1024)}
+    out = {}
+    for name, ((speed, seeds), block, n) in cases.items():
+        d_speed = torch.from_numpy(speed).to(dev)
+        d_seeds = torch.from_numpy(seeds.astype(np.int32)).to(dev)
+        d_time = torch.empty_like(d_speed)
+        row = {}
+        for kname, kern in (("systolic", g.Kernel.Systolic), ("fim", g.Kernel.FIM)):
+            with g.HcmSetup(g.HcmConfig(block_size=block, max_jobs=n, fim_minimum_change=EPS, kernel=kern)) as s:
+                ms, sts = timed_device_solves(g, s, d_speed, d_seeds, d_time, stream, flush, steps, 1)
+            row[kname] = {"ms": ms, "mcells": speed.size / (ms * 1e3),
+                          "block_solves": statistics.mean(x["block_solves"] for x in sts),
+                          "waves": statistics.mean(x["waves"] for x in sts),
+                          "sweeps_note": "block-FIM counts one open-set iteration as a sweep"}
+        row["faster"] = min(("systolic", "fim"), key=lambda k: row[k]["ms"])
+        out[name] = row
+    return out
+
+
 def run_batched(args, world, rank, local) -> int:
     """C4: the batch of independent instances in one persistent launch from a
     CUDA graph, configured by the autotuner; ranks split the instances."""
@@ -567,16 +605,26 @@ def run_batched(args, world, rank, local) -> int:
     return 0
 
 
+def maze_model(block: int):
+    """The schedule model trained on maze traces for tiles of `block`, if present."""
+    p = ROOT / "ghcm_gb300" / "models" / f"schedule_maze4096_b{block}.npz"
+    return p if p.exists() else None
+
+
 def run_maze(args, world, rank, local) -> int:
     """C5: the 16384^2 cellular-automaton maze (wall speed 0.001, open 1.0, 64
-    sources in open cells, ~2 GB of device state): a short tile-size / n sweep,
-    the best timed, and the error against an FP64 FMM of the whole field
-    reported on the central 2048^2 crop."""
+    sources in open cells, ~2 GB of device state). The library's autotuner
+    (ghcm_autotune_batch, on the field as a batch of one) picks tile size, n,
+    sweep cap and tile kernel; the learned schedule (a model trained on maze
+    traces for that tile size) is timed against the plain schedule at that
+    config. `value` is the learned schedule's Mcell/s; both fields are
+    checked against the reference FIM, and against an FP64 FMM of the whole
+    field (errors on the whole field and on the central 2048^2 crop)."""
     import torch
 
     import ghcm_gb300 as g
-    from ghcm_gb300 import fields
-    from oracle.oracle import Oracle, build
+    from ghcm_gb300 import fields, learned
+    from oracle.oracle import Oracle, build, rel_diff
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -589,52 +637,75 @@ def run_maze(args, world, rank, local) -> int:
     d_seeds = torch.from_numpy(seeds.astype(np.int32)).to(dev)
     d_time = torch.empty_like(d_speed)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    sweep = {}
-    best = None
-    for block, n in ((16, 4096), (16, 16384), (32, 4096), (32, 16384)):
-        cfg = g.HcmConfig(block_size=block, max_jobs=n, fim_minimum_change=EPS)
-        with g.HcmSetup(cfg) as s:
-            ms, sts = timed_device_solves(g, s, d_speed, d_seeds, d_time, stream, flush, 1, 1)
-        sweep[f"b{block}_n{n}"] = {"ms": ms, "mcells": cells / (ms * 1e3), "block_solves": sts[0]["block_solves"],
-                                   "waves": sts[0]["waves"]}
-        if best is None or ms < best[2]:
-            best = (block, n, ms)
-    block, n, _ = best
-    setup = g.HcmSetup(g.HcmConfig(block_size=block, max_jobs=n, fim_minimum_change=EPS))
+    t0 = time.perf_counter()
+    tuned, trials = g.autotune_batch(g.HcmConfig(block_size=16, fim_minimum_change=EPS),
+                                     [g.DeviceInstance(d_speed, d_seeds, d_time)], reps=1)
+    tune_s = time.perf_counter() - t0
+    block, n = tuned.block_size, tuned.max_jobs
+    plain_cfg = g.HcmConfig(block_size=block, max_jobs=n, max_sweeps=tuned.max_sweeps, kernel=tuned.kernel,
+                            fim_minimum_change=EPS)
+    s_plain = g.HcmSetup(plain_cfg)
+    mpath = maze_model(block)
+    s_learned = None
+    if mpath is not None and tuned.kernel == g.Kernel.Systolic:
+        params, threshold, meta = learned.load_model(mpath)
+        s_learned = _learned_setup(g, learned, params, threshold, learned.POLICY_SCORE, max_jobs=n,
+                                   fallback_jobs=n, max_sweeps=tuned.max_sweeps)
+    head = s_learned if s_learned is not None else s_plain
+    d_time_p = torch.empty_like(d_speed)
     with Clocks(local) as clk:
-        ms, stats = timed_device_solves(g, setup, d_speed, d_seeds, d_time, stream, flush, args.steps, args.warmup)
+        ms, stats = timed_device_solves(g, head, d_speed, d_seeds, d_time, stream, flush, args.steps, args.warmup)
+        pms, pstats = timed_device_solves(g, s_plain, d_speed, d_seeds, d_time_p, stream, flush, args.steps,
+                                          args.warmup)
     clocks = clk.summary()
     value = cells / (ms * 1e3)
     h_speed = torch.from_numpy(speed).pin_memory()
     h_time = torch.empty_like(h_speed).pin_memory()
-    g.eikonal_hcm_cuda_ex(setup, h_speed.numpy(), seeds, input_is_speed=True, out=h_time.numpy())  # warm-up
+    g.eikonal_hcm_cuda_ex(head, h_speed.numpy(), seeds, input_is_speed=True, out=h_time.numpy())  # warm-up
     e2e = []
     for _ in range(2):
         t0 = time.perf_counter()
-        g.eikonal_hcm_cuda_ex(setup, h_speed.numpy(), seeds, input_is_speed=True, out=h_time.numpy())
+        g.eikonal_hcm_cuda_ex(head, h_speed.numpy(), seeds, input_is_speed=True, out=h_time.numpy())
         e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = min(e2e)
-    g.solve_device(setup, d_speed, d_seeds, d_time, stream=stream)
+    g.solve_device(head, d_speed, d_seeds, d_time, stream=stream)
+    g.solve_device(s_plain, d_speed, d_seeds, d_time_p, stream=stream)
     field = d_time.cpu().numpy()
+    field_p = d_time_p.cpu().numpy()
+    del d_time, d_time_p
     solves = statistics.mean(st["block_solves"] for st in stats)
     k_ms = statistics.mean(st["kernel_ms"] for st in stats)
     achieved = solves * bytes_per_solve(block) / (k_ms * 1e-3) / 1e9
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)
+    capture = load_traffic("k_solve_maze16384.json", block=block, n=n)
+    cap_solves = load_block_solves("k_solve_maze16384.json")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": MAZE_WORKLOAD, "seed": MAZE_SEED, "block": block, "n": n, "eps": EPS,
-                   "sources": int(len(seeds)), "generate_s": gen_s,
-                   "device_state_gb": 2 * 4 * cells / 1e9, "l2": "flushed between steps"},
+        "config": {"workload": MAZE_WORKLOAD, "seed": MAZE_SEED, "block": block, "n": n,
+                   "max_sweeps": tuned.max_sweeps, "kernel": "fim" if tuned.kernel == g.Kernel.FIM else "systolic",
+                   "schedule": "learned (score policy)" if s_learned is not None else "plain",
+                   "model": mpath.name if mpath is not None else None, "eps": EPS, "sources": int(len(seeds)),
+                   "generate_s": gen_s, "autotune_s": tune_s, "device_state_gb": 2 * 4 * cells / 1e9,
+                   "l2": "flushed between steps"},
+        "plain": {"value": cells / (pms * 1e3), "unit": UNIT, "ms_per_step": pms,
+                  "block_solves": statistics.mean(st["block_solves"] for st in pstats),
+                  "waves": statistics.mean(st["waves"] for st in pstats)},
+        "learned_vs_plain": {"mcells_ratio": pms / ms,
+                             "block_solves_ratio": solves / statistics.mean(st["block_solves"] for st in pstats)},
         "e2e": {"value": cells / (e2e_ms * 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": 4 * cells + int(seeds.nbytes), "d2h_bytes_per_step": 4 * cells},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": f"k_solve<{block},systolic>", "bytes_per_block_solve":
-                         bytes_per_solve(block), "block_solves": solves, "kernel_ms": k_ms},
-        "sweep": sweep,
-        "gpu_launches": LAUNCHES_PER_SOLVE * args.steps,
+                     "traffic": (capture / cap_solves * solves) if capture and cap_solves else None,
+                     "traffic_basis": "DRAM bytes per block-solve of an ncu capture of the plain maze launch at the "
+                                      "same tile size and n (profiles/k_solve_maze16384.json) x this run's "
+                                      "block-solves",
+                     "kernel": f"k_solve<{block},{'fim' if tuned.kernel == g.Kernel.FIM else 'systolic'}>",
+                     "bytes_per_block_solve": bytes_per_solve(block), "block_solves": solves, "kernel_ms": k_ms},
+        "autotune": trials,
+        "gpu_launches": (LAUNCHES_PER_LEARNED_SOLVE if s_learned is not None else LAUNCHES_PER_SOLVE) * args.steps,
         "clocks": clocks,
         "solver": {"waves": statistics.mean(st["waves"] for st in stats),
                    "residual_passes": statistics.mean(st["residual_passes"] for st in stats),
@@ -645,20 +716,27 @@ def run_maze(args, world, rank, local) -> int:
         o = Oracle()
         cost = fields.cost_from_speed(speed)
         line["check"] = {"residual": o.residual(cost, field), "finite": bool(np.isfinite(field).all()),
-                         "seeds_zero": bool(np.all(field[seeds[:, 1], seeds[:, 0]] == 0))}
+                         "seeds_zero": bool(np.all(field[seeds[:, 1], seeds[:, 0]] == 0)),
+                         "learned_vs_plain_max_rel": rel_diff(field, field_p)}
         if not args.no_cpu_baseline:
-            t0 = time.perf_counter()
+            fim, us_fim = o.fim(cost, seeds, EPS)
+            line["check"]["max_rel_vs_fim"] = rel_diff(field, fim)
+            line["check"]["plain_max_rel_vs_fim"] = rel_diff(field_p, fim)
+            del fim
             ref64, us64 = o.fmm64(cost, seeds)
             c0 = (16384 - MAZE_CROP) // 2
             crop = (slice(c0, c0 + MAZE_CROP), slice(c0, c0 + MAZE_CROP))
             line["check"]["vs_fmm64_crop"] = {**fmm64_errors(field[crop], ref64[crop]),
                                               "crop": f"[{c0}:{c0 + MAZE_CROP}]^2"}
             line["check"]["vs_fmm64_full"] = fmm64_errors(field, ref64)
-            line["cpu_baseline"] = {"value": cells / us64, "unit": UNIT, "cores": 1, "kind": "port",
-                                    "sample": "one FP64 FMM of the whole field (the accuracy oracle), 1 host thread",
-                                    "cpu": _cpu_name()}
+            line["check"]["plain_vs_fmm64_full"] = fmm64_errors(field_p, ref64)
+            line["cpu_baseline"] = {"value": cells / us_fim, "unit": UNIT, "cores": 1, "kind": "port",
+                                    "sample": "one reference FIM of the whole field (eps 1e-5), 1 host thread",
+                                    "fmm64_ms": us64 / 1e3, "cpu": _cpu_name()}
         print(json.dumps(line), flush=True)
-    setup.close()
+    if s_learned is not None:
+        s_learned.close()
+    s_plain.close()
     return 0
 
 
@@ -1007,6 +1085,8 @@ def run_noise(args, world, rank, local) -> int:
             line["ring_4096"] = ring_4096(g, dev, stream, flush, k, 1, checks=not args.no_cpu_baseline)
         if not args.no_cpu_baseline and not args.quick:
             line["small_ring_256"] = small_ring_check(g)
+        if not args.quick:
+            line["kernels"] = kernel_compare(g, dev, stream, flush, k)
         print(json.dumps(line), flush=True)
     s_learned.close()
     s_plain.close()

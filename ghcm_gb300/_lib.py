@@ -142,6 +142,8 @@ class GhcmTuneTrial(ctypes.Structure):
         ("status", ctypes.c_int32),
         ("ms", ctypes.c_double),
         ("block_solves", ctypes.c_uint64),
+        ("kernel", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:

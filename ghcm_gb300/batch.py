@@ -24,7 +24,7 @@ from typing import Callable, Sequence
 
 from . import _lib
 from ._lib import GhcmError, GhcmStats
-from .eikonal import HcmConfig, HcmSetup
+from .eikonal import HcmConfig, HcmSetup, Kernel
 
 
 @dataclass
@@ -139,8 +139,9 @@ def solve_batched(setup: HcmSetup, instances: Sequence[DeviceInstance], stream=N
 
 
 def autotune_batch(config: HcmConfig, instances: Sequence[DeviceInstance], stream=None, reps: int = 2):
-    """Times the batch under tile sizes 8/16/32, n and inner-sweep caps
-    (ghcm_autotune_batch) and returns (best HcmConfig, list of trial dicts).
+    """Times the batch under tile sizes 8/16/32, n, inner-sweep caps and both
+    tile kernels (ghcm_autotune_batch) and returns (best HcmConfig, list of
+    trial dicts).
     The instances' time tensors hold a converged solve afterwards."""
     base = config.to_c()
     best = _lib.GhcmConfig()
@@ -156,6 +157,7 @@ def autotune_batch(config: HcmConfig, instances: Sequence[DeviceInstance], strea
     tuned.block_size = int(best.block_size)
     tuned.max_jobs = int(best.max_jobs)
     tuned.max_sweeps = int(best.max_sweeps)
+    tuned.kernel = Kernel(int(best.kernel))
     return tuned, [trials[i].as_dict() for i in range(min(n.value, 64))]
 
 

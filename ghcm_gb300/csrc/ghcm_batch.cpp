@@ -191,6 +191,7 @@ int ghcm_batch_create(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count,
     };
     size_t const t4 = sizeof(uint32_t) * b->tiles;
     size_t const o_flags = take(t4), o_key = take(t4), o_tmin = take(t4), o_l0 = take(t4), o_l1 = take(t4);
+    size_t const o_epoch = take(t4);
     size_t const o_ti = take(t4), o_jobs = take(sizeof(uint32_t) * std::max<uint32_t>(s.max_jobs, 1u));
     size_t const o_ctl = take(sizeof(Ctl)), o_insts = take(sizeof(Inst) * count);
     size_t const o_maps = take(sizeof(CUtensorMap) * 2u * count);
@@ -211,6 +212,7 @@ int ghcm_batch_create(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count,
     s.flags = reinterpret_cast<uint32_t*>(base + o_flags);
     s.key = reinterpret_cast<uint32_t*>(base + o_key);
     s.tmin = reinterpret_cast<float*>(base + o_tmin);
+    s.epoch = reinterpret_cast<uint32_t*>(base + o_epoch);
     s.list[0] = reinterpret_cast<uint32_t*>(base + o_l0);
     s.list[1] = reinterpret_cast<uint32_t*>(base + o_l1);
     s.tile_inst = reinterpret_cast<const uint32_t*>(base + o_ti);
@@ -321,12 +323,13 @@ int ghcm_autotune_batch(const ghcm_config* base, const ghcm_instance* insts, uin
     } pick{*base, 0.0, false};
 
     // one trial: fresh context and batch, a warm-up replay, then the best of reps
-    auto trial = [&](uint32_t B, uint32_t n, uint32_t sweeps) {
+    auto trial = [&](uint32_t B, uint32_t n, uint32_t sweeps, uint32_t kernel) {
         ghcm_config c = *base;
         c.block_size = B;
         c.max_jobs = n;
         c.max_sweeps = sweeps;
-        ghcm_tune_trial t{B, n, sweeps, GHCM_OK, 0.0, 0ull};
+        c.kernel = kernel;
+        ghcm_tune_trial t{B, n, sweeps, GHCM_OK, 0.0, 0ull, kernel, 0u};
         ghcm_ctx* ctx = nullptr;
         ghcm_batch* b = nullptr;
         int r = ghcm_create(&c, &ctx);
@@ -350,19 +353,22 @@ int ghcm_autotune_batch(const ghcm_config* base, const ghcm_instance* insts, uin
     };
 
     // stage 1: tile size x n on a coarse grid; stage 2: n halved and doubled
-    // around the best; stage 3: inner-sweep caps
+    // around the best; stage 3: inner-sweep caps; stage 4: the other tile
+    // kernel (systolic <-> block-FIM, data/eikonal_ghcm_fim.cl:214-392)
     uint32_t const S = static_cast<uint32_t>(sms);
+    uint32_t const K = base->kernel;
     for (uint32_t B : {8u, 16u, 32u})
-        for (uint32_t m : {4u, 16u, 64u}) trial(B, m * S, 0u);
+        for (uint32_t m : {4u, 16u, 64u}) trial(B, m * S, 0u, K);
     if (!pick.ok) {
         if (n_trials) *n_trials = ran;
         return GHCM_ERR_INTERNAL;
     }
     uint32_t const bB = pick.cfg.block_size;
     uint32_t const n1 = pick.cfg.max_jobs;
-    for (uint32_t n : {n1 / 2u, n1 * 2u}) trial(bB, n, 0u);
+    for (uint32_t n : {n1 / 2u, n1 * 2u}) trial(bB, n, 0u, K);
     uint32_t const bN = pick.cfg.max_jobs;
-    for (uint32_t sw : {bB / 2u, bB, 2u * bB}) trial(bB, bN, sw);
+    for (uint32_t sw : {bB / 2u, bB, 2u * bB}) trial(bB, bN, sw, K);
+    trial(bB, bN, pick.cfg.max_sweeps, K == GHCM_KERNEL_FIM ? GHCM_KERNEL_SYSTOLIC : GHCM_KERNEL_FIM);
     // leave the fastest config's solve in the outputs
     ghcm_ctx* ctx = nullptr;
     rc = ghcm_create(&pick.cfg, &ctx);

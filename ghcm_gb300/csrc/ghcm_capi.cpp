@@ -69,7 +69,7 @@ bool encode_tile_map(EncodeTiledFn encode, CUtensorMap* map, const float* base, 
 namespace {
 
 struct Layout {
-    size_t flags, key, tmin, list0, list1, jobs, ctl, insts, total;
+    size_t flags, key, tmin, epoch, list0, list1, jobs, ctl, insts, total;
 };
 
 Layout layout_for(uint32_t tiles, uint32_t jobs) {
@@ -83,6 +83,7 @@ Layout layout_for(uint32_t tiles, uint32_t jobs) {
     l.flags = take(sizeof(uint32_t) * tiles);
     l.key = take(sizeof(uint32_t) * tiles);
     l.tmin = take(sizeof(float) * tiles);
+    l.epoch = take(sizeof(uint32_t) * tiles);
     l.list0 = take(sizeof(uint32_t) * tiles);
     l.list1 = take(sizeof(uint32_t) * tiles);
     l.jobs = take(sizeof(uint32_t) * std::max<uint32_t>(jobs, 1));
@@ -134,6 +135,7 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     s.flags = reinterpret_cast<uint32_t*>(base + L.flags);
     s.key = reinterpret_cast<uint32_t*>(base + L.key);
     s.tmin = reinterpret_cast<float*>(base + L.tmin);
+    s.epoch = reinterpret_cast<uint32_t*>(base + L.epoch);
     s.list[0] = reinterpret_cast<uint32_t*>(base + L.list0);
     s.list[1] = reinterpret_cast<uint32_t*>(base + L.list1);
     s.jobs = reinterpret_cast<uint32_t*>(base + L.jobs);

@@ -127,6 +127,7 @@ struct Sched {
     uint32_t* flags;               // per-tile kActive | kFull | edge bits
     uint32_t* key;                 // per-tile priority key (float bits; +inf = none)
     float*    tmin;                // per-tile smallest time after the last solve
+    uint32_t* epoch;               // per tile: the residual pass its last changing solve came before (0: none)
     uint32_t* list[2];             // active lists, capacity num_tiles each
     uint32_t* jobs;                // selected jobs, capacity max_jobs
     Ctl*      ctl;

@@ -11,7 +11,7 @@
 // smallest times, the two active lists, the job list, the control block and
 // the instance record - lives in one file-scope __device__ array below, sized
 // for at most GHCM_NOALLOC_MAX_TILES tiles. Every GPU that loads the library
-// holds that array (about 6 MiB) until the process exits.
+// holds that array (about 7 MiB) until the process exits.
 //
 // The caller passes the field, seeds and output on the device, as for
 // ghcm_solve_device. Calls share the one array: two calls that overlap on the
@@ -35,8 +35,8 @@ namespace {
 constexpr size_t kSlot = static_cast<size_t>(GHCM_NOALLOC_MAX_TILES) * sizeof(uint32_t);
 constexpr size_t kCtlBytes = 2048;
 constexpr size_t kInstBytes = 256;
-// flags | key | tmin | list0 | list1 | jobs | control block | instance
-constexpr size_t kScratchBytes = 6 * kSlot + kCtlBytes + kInstBytes;
+// flags | key | tmin | list0 | list1 | jobs | epoch | control block | instance
+constexpr size_t kScratchBytes = 7 * kSlot + kCtlBytes + kInstBytes;
 static_assert(sizeof(Ctl) <= kCtlBytes && sizeof(Inst) <= kInstBytes, "scratch slots too small");
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -124,8 +124,9 @@ extern "C" int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_
     s.list[0] = reinterpret_cast<uint32_t*>(base + 3 * kSlot);
     s.list[1] = reinterpret_cast<uint32_t*>(base + 4 * kSlot);
     s.jobs = reinterpret_cast<uint32_t*>(base + 5 * kSlot);
-    s.ctl = reinterpret_cast<Ctl*>(base + 6 * kSlot);
-    Inst* d_inst = reinterpret_cast<Inst*>(base + 6 * kSlot + kCtlBytes);
+    s.epoch = reinterpret_cast<uint32_t*>(base + 6 * kSlot);
+    s.ctl = reinterpret_cast<Ctl*>(base + 7 * kSlot);
+    Inst* d_inst = reinterpret_cast<Inst*>(base + 7 * kSlot + kCtlBytes);
     s.insts = d_inst;
     s.tile_inst = nullptr;
     s.num_tiles = tiles;

@@ -289,7 +289,10 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
 
 // The scheduler state each CTA keeps in shared memory (s_state[]), refreshed
 // from the release word at every wave barrier.
-enum : int { kStPhase = 0, kStCur = 1, kStJobs = 2, kStInList = 3, kStError = 4, kStWaves = 5, kStGen = 6 };
+enum : int {
+    kStPhase = 0, kStCur = 1, kStJobs = 2, kStInList = 3, kStError = 4, kStWaves = 5, kStGen = 6,
+    kStResid = 7,  // residual passes begun
+};
 
 // Release word: the decision of the last CTA, published with the release.
 //   bits 0-31 job count, 32-35 phase, 36 cur, 37 jobs-in-list, 38 error,
@@ -311,6 +314,7 @@ __device__ __forceinline__ void unpack_release(unsigned long long w, uint32_t* s
     st[kStError] = static_cast<uint32_t>(w >> 38) & 1u;
     st[kStGen] = static_cast<uint32_t>(w >> 40) & 0xffffffu;
     if (phase == kPhaseJobs) st[kStWaves] += 1u;
+    if (phase == kPhaseResidual) st[kStResid] += 1u;
 }
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {

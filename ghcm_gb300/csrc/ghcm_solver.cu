@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, CTAS) k_solve(const __gr
                     break;
                 }
                 int const r = solve_tile<B, FIM>(s, job, cur ^ 1u, sm, &s_bar, parity, tma_pending, s_word, s_red,
-                                                 s_krange, wave);
+                                                 s_krange, wave, s_state[kStResid] + 1u);
                 if (r == kJobFailed) break;
                 solves += (r == kJobSolved) ? 1u : 0u;
             }
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, CTAS) k_solve(const __gr
             GHCM_PROF_END(ctl, 1, t_solve);
         } else if (phase == kPhaseResidual) {
             GHCM_PROF_BEGIN(t_res);
-            residual_warp<B>(s, cur ^ 1u, gw, nwarps, s_krange);
+            residual_warp<B>(s, cur ^ 1u, gw, nwarps, s_krange, s_state[kStResid]);
             GHCM_PROF_END(ctl, 4, t_res);
         } else {
             break;  // done or stopped
@@ -221,14 +221,15 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
                     if (lane == 0) atomicOr(&ctl->error, kErrInternal);
                     break;
                 }
-                int const r = solve_tile_warp<B>(s, job, cur ^ 1u, sm, parity, tma_pending, s_krange, wave);
+                int const r = solve_tile_warp<B>(s, job, cur ^ 1u, sm, parity, tma_pending, s_krange, wave,
+                                                 s_state[kStResid] + 1u);
                 if (r == kJobFailed) break;
                 solves += (r == kJobSolved) ? 1u : 0u;
             }
             GHCM_PROF_END(ctl, 1, t_solve);
         } else if (phase == kPhaseResidual) {
             GHCM_PROF_BEGIN(t_res);
-            residual_warp<B>(s, cur ^ 1u, gw, nwarps, s_krange);
+            residual_warp<B>(s, cur ^ 1u, gw, nwarps, s_krange, s_state[kStResid]);
             GHCM_PROF_END(ctl, 4, t_res);
         } else {
             break;  // done or stopped
@@ -256,6 +257,7 @@ __global__ void k_init_inst(Sched s) {
     for (uint32_t t = first; t < n_tiles; t += stride) {
         uint32_t const g = I.tile_base + t;
         s.flags[g] = 0u;
+        s.epoch[g] = 0u;
         s.key[g] = inf_bits();
         s.tmin[g] = f_inf();
         if (s.tile_inst) const_cast<uint32_t*>(s.tile_inst)[g] = blockIdx.y;

@@ -75,7 +75,7 @@ enum : int { kJobFailed = 0, kJobSolved = 1, kJobDeferred = 2 };
 template <int B, bool FIM>
 __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<B>& sm, uint64_t* bar,
                            uint32_t& parity, bool& tma_pending, uint32_t* s_word, float* s_red, uint32_t* s_krange,
-                           uint32_t wave) {
+                           uint32_t wave, uint32_t epoch) {
     using G = TileGeom<B>;
     int const tid = threadIdx.x;
     uint32_t const ii = inst_of(s, tile);
@@ -390,6 +390,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         float m = s_red[0];
         for (int w = 1; w < G::THREADS / 32; ++w) m = fminf(m, s_red[w]);
         s.tmin[tile] = m;
+        if (tile_changed) s.epoch[tile] = epoch;  // the next residual pass re-checks it and its neighbours
         if (solve_count(flags) < s.refresh && !(s_word[4] & 16u)) atomicAdd(&s.flags[tile], kSolveOne);
         learn_commit(s, tile, useful, wave, sweeps, sm.feat);
         if (capped) activate(s, tile, kFull, m, nxt, s_krange);
@@ -425,14 +426,29 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
 }
 
 // Global residual check, one tile per warp: re-activates every tile holding
-// a cell whose Godunov update would still lower it by more than eps. The
-// reference has no such check (src/eikonal_hcm.cpp:343, 486-488).
+// a cell whose Godunov update would still move it by more than eps. Pass
+// `pass` (1-based) re-checks only tiles that changed, or have a neighbour that
+// changed, since the pass before it (epoch >= pass): a cell's update reads
+// only the cell and its four neighbours, so a tile with no change around it
+// keeps the residual the previous pass found clean. The reference has no such
+// check (src/eikonal_hcm.cpp:343, 486-488).
 template <int B>
-__device__ void residual_warp(const Sched& s, uint32_t nxt, uint32_t warp_global, uint32_t warps, uint32_t* s_krange) {
+__device__ void residual_warp(const Sched& s, uint32_t nxt, uint32_t warp_global, uint32_t warps, uint32_t* s_krange,
+                              uint32_t pass) {
     int const lane = threadIdx.x & 31;
     for (uint32_t tile = warp_global; tile < s.num_tiles; tile += warps) {
         const Inst& I = s.insts[inst_of(s, tile)];
         TileCoord const tc = tile_coord<B>(I, tile);
+        {
+            uint32_t ep = 0u;
+            if (lane < 4) {
+                int const nb = neighbour_tile(I, tc.tx, tc.ty, lane);
+                if (nb >= 0) ep = __ldcg(&s.epoch[nb]);
+            } else if (lane == 4) {
+                ep = __ldcg(&s.epoch[tile]);
+            }
+            if (!__any_sync(0xffffffffu, ep >= pass)) continue;
+        }
         bool const fresh = solve_count(ld_relaxed(&s.flags[tile])) < s.refresh;
         bool bad = false;
         float kmin = f_inf();

@@ -42,7 +42,7 @@ struct alignas(128) WarpTileSmem {
 // timed out).
 template <int B>
 __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, WarpTileSmem<B>& sm, uint32_t& parity,
-                                bool& tma_pending, uint32_t* s_krange, uint32_t wave) {
+                                bool& tma_pending, uint32_t* s_krange, uint32_t wave, uint32_t epoch) {
     using G = TileGeom<B>;
     using W = WarpTileGeom<B>;
     constexpr unsigned FULL = 0xffffffffu;
@@ -247,6 +247,7 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     __syncwarp();
     if (lane == 0) {
         s.tmin[tile] = lmin;
+        if (tile_changed) s.epoch[tile] = epoch;  // the next residual pass re-checks it and its neighbours
         if (solve_count(sm.claim[0]) < s.refresh && !(ec & 16u)) atomicAdd(&s.flags[tile], kSolveOne);
         learn_commit(s, tile, useful, wave, sweeps, sm.feat);
 #pragma unroll

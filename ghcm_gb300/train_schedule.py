@@ -1,12 +1,15 @@
 """Trains the learned block schedule on traces of the plain solver.
 
-    python -m ghcm_gb300.train_schedule [--size 4096] [--seeds 32] [--first-seed 1001]
-                                         [--n 1024] [--epochs 12] [--out FILE]
+    python -m ghcm_gb300.train_schedule [--field noise|maze] [--size 4096] [--seeds 32]
+                                         [--first-seed 1001] [--block 16] [--n 1024]
+                                         [--epochs 12] [--out FILE]
 
 For each training seed: a fractal value-noise speed field (6 octaves, base
 period size/8, persistence 0.5, speed = clamp(exp(2 noise), 0.02, 1)) with 16
-random sources is solved by the plain device schedule (tiles of 16, n = --n)
-with the trace recorder on. Each block-solve's features are labelled with the
+random sources, or (--field maze) a cellular-automaton maze (walls at speed
+0.001, open cells 1.0, 5 smoothing passes) with 64 sources in open cells, is
+solved by the plain device schedule (tiles of --block, n = --n) with the trace
+recorder on. Each block-solve's features are labelled with the
 hindsight target of learned.final_labels (the solve moved some cell by more
 than eps and no later solve of its tile did); the 12 -> 64 -> 64 -> 1 MLP is
 trained by the library's CUDA kernels and written with its metadata to --out.
@@ -30,12 +33,15 @@ DEFAULT_OUT = Path(__file__).resolve().parent / "models" / "schedule_noise4096_b
 def _field(args):
     from ghcm_gb300 import fields
 
-    size, seed = args
+    kind, size, seed = args
+    if kind == "maze":
+        return seed, fields.ca_maze(size, seed=seed, sources=64)
     return seed, fields.value_noise(size, seed=seed, base_period=size / 8.0, sources=16)
 
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--field", default="noise", choices=["noise", "maze"])
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--seeds", type=int, default=32)
     ap.add_argument("--first-seed", type=int, default=1001)
@@ -51,7 +57,7 @@ def main(argv=None) -> int:
     seeds = list(range(args.first_seed, args.first_seed + args.seeds))
     t0 = time.perf_counter()
     with ProcessPoolExecutor(max_workers=max(1, args.workers), mp_context=get_context("spawn")) as ex:
-        made = dict(ex.map(_field, [(args.size, s) for s in seeds]))
+        made = dict(ex.map(_field, [(args.field, args.size, s) for s in seeds]))
     t_gen = time.perf_counter() - t0
 
     import ghcm_gb300 as g
@@ -85,7 +91,7 @@ def main(argv=None) -> int:
     }
     args.out.parent.mkdir(parents=True, exist_ok=True)
     learned.save_model(args.out, params, args.threshold, train_seeds=np.array(seeds), size=args.size,
-                       block=args.block, trace_n=args.n, label="final", epoch_loss=np.array(losses),
+                       field=args.field, block=args.block, trace_n=args.n, label="final", epoch_loss=np.array(losses),
                        summary=json.dumps(summary))
     print(json.dumps({"model": str(args.out), **summary}))
     return 0

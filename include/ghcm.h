@@ -196,12 +196,15 @@ typedef struct ghcm_tune_trial {
     int32_t  status;                /* GHCM_OK or the failing status */
     double   ms;                    /* best device time of the replays */
     uint64_t block_solves;
+    uint32_t kernel;                /* GHCM_KERNEL_* */
+    uint32_t reserved;
 } ghcm_tune_trial;
 
-/* Picks tile size (8, 16, 32), n and the inner-sweep cap for a batch by
- * timing CUDA-graph replays of it, starting from `base`: tile size x n on the
- * grid {8, 16, 32} x {4, 16, 64} x SMs, then n halved and doubled around the
- * best, then the inner-sweep caps B/2, B, 2B (14 trials).
+/* Picks tile size (8, 16, 32), n, the inner-sweep cap and the tile kernel
+ * for a batch by timing CUDA-graph replays of it, starting from `base` (its
+ * kernel): tile size x n on the grid {8, 16, 32} x {4, 16, 64} x SMs, then n
+ * halved and doubled around the best, then the inner-sweep caps B/2, B, 2B,
+ * then the best config with the other tile kernel (15 trials).
  * Writes the fastest config to *best and the trials run to
  * trials[0..max_trials) (*n_trials = how many ran; trials may be NULL). The
  * instances' time_out fields hold a converged solve on return. reps >= 1
@@ -323,7 +326,7 @@ int ghcm_abi_version(void);
  * a library do it - a host whose pool owns every device allocation, a path that
  * must not synchronise the device the way cudaMalloc/cudaFree can, a service
  * whose footprint must not grow after start-up. The scheduler's scratch is one
- * static device array of about 6 MiB that every GPU loading the library holds
+ * static device array of about 7 MiB that every GPU loading the library holds
  * until exit; fields whose tiling exceeds GHCM_NOALLOC_MAX_TILES are rejected
  * with GHCM_ERR_TOO_LARGE. Runs on the current device (cfg->device must be -1
  * or that device) on `stream` and returns when the solve has finished.

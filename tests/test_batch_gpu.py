@@ -146,10 +146,11 @@ def test_autotuner_picks_a_working_config(dev, oracle_lib):
     dinst = _to_device(insts, dev)
     best, trials = g.autotune_batch(g.HcmConfig(block_size=16), dinst, reps=1)
     assert best.block_size in (8, 16, 32)
-    assert len(trials) == 14
+    assert len(trials) == 15
     assert all(t["status"] == 0 for t in trials)
+    assert {t["kernel"] for t in trials} == {int(g.Kernel.Systolic), int(g.Kernel.FIM)}
     ok = [t for t in trials if t["block_size"] == best.block_size and t["max_jobs"] == best.max_jobs
-          and t["max_sweeps"] == best.max_sweeps]
+          and t["max_sweeps"] == best.max_sweeps and t["kernel"] == int(best.kernel)]
     assert ok and ok[0]["ms"] == min(t["ms"] for t in trials)
     for inst, di in zip(insts, dinst):
         ref = oracle_lib.fim(fields.cost_from_speed(inst.speed), inst.seeds, 1e-5)[0]
