@@ -300,6 +300,10 @@ int ghcm_solve_batched(ghcm_ctx* ctx, const ghcm_instance* insts, uint32_t count
     return rc;
 }
 
+// Wave cap of one autotuner trial (a wave takes at least ~10 us, so a trial
+// ends within seconds even on a config that would not converge).
+constexpr uint32_t kTuneWaveCap = 200000u;
+
 int ghcm_autotune_batch(const ghcm_config* base, const ghcm_instance* insts, uint32_t count, void* stream,
                         uint32_t reps, ghcm_config* best, ghcm_tune_trial* trials, uint32_t max_trials,
                         uint32_t* n_trials) {
@@ -329,6 +333,9 @@ int ghcm_autotune_batch(const ghcm_config* base, const ghcm_instance* insts, uin
         c.max_jobs = n;
         c.max_sweeps = sweeps;
         c.kernel = kernel;
+        // a trial may not run unbounded: a config that cannot finish fails with
+        // GHCM_ERR_NOT_CONVERGED and is skipped
+        if (c.max_waves == 0u) c.max_waves = kTuneWaveCap;
         ghcm_tune_trial t{B, n, sweeps, GHCM_OK, 0.0, 0ull, kernel, 0u};
         ghcm_ctx* ctx = nullptr;
         ghcm_batch* b = nullptr;
@@ -375,6 +382,7 @@ int ghcm_autotune_batch(const ghcm_config* base, const ghcm_instance* insts, uin
     if (rc == GHCM_OK) rc = ghcm_solve_batched(ctx, insts, count, stream, nullptr);
     if (ctx) ghcm_destroy(ctx);
     *best = pick.cfg;
+    best->max_waves = base->max_waves;
     if (n_trials) *n_trials = ran;
     return rc;
 }

@@ -199,9 +199,13 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     // (kUpdFresh: a value an earlier solve rounded low rises again and the
     // neighbours are told). Past fresh_sweeps sweeps, and for the reference
     // form, cells only fall (kUpdKeepMin); the limits end the one-ulp
-    // oscillations of nearly tied neighbours.
+    // oscillations of nearly tied neighbours. fresh_sweeps is at most half
+    // the sweep cap, so every solve ends with sweeps that only lower cells,
+    // and a solve the cap stops counts against the budget like a quiet one:
+    // otherwise a cap below fresh_sweeps would re-queue an oscillating tile
+    // forever.
     int mode = solve_count(flags) < s.refresh ? kUpdFresh : (s.in_solve ? kUpdInSolve : kUpdKeepMin);
-    uint32_t const fresh_sweeps = 4u * B;
+    uint32_t const fresh_sweeps = min(4u * B, max(1u, s.max_sweeps / 2u));
     bool own_changed = false;
     bool capped = false;
     uint32_t sweeps = 0;
@@ -391,7 +395,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         for (int w = 1; w < G::THREADS / 32; ++w) m = fminf(m, s_red[w]);
         s.tmin[tile] = m;
         if (tile_changed) s.epoch[tile] = epoch;  // the next residual pass re-checks it and its neighbours
-        if (solve_count(flags) < s.refresh && !(s_word[4] & 16u)) atomicAdd(&s.flags[tile], kSolveOne);
+        if (solve_count(flags) < s.refresh && (capped || !(s_word[4] & 16u))) atomicAdd(&s.flags[tile], kSolveOne);
         learn_commit(s, tile, useful, wave, sweeps, sm.feat);
         if (capped) activate(s, tile, kFull, m, nxt, s_krange);
     }

@@ -124,7 +124,7 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     float const eps = s.eps;
     // how sweeps bound the update (see solve_tile)
     int mode = solve_count(sm.claim[0]) < s.refresh ? kUpdFresh : (s.in_solve ? kUpdInSolve : kUpdKeepMin);
-    uint32_t const fresh_sweeps = 4u * B;
+    uint32_t const fresh_sweeps = min(4u * B, max(1u, s.max_sweeps / 2u));  // see solve_tile
     bool changed = false;
     bool capped = false;
     uint32_t sweeps = 0;
@@ -248,7 +248,7 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     if (lane == 0) {
         s.tmin[tile] = lmin;
         if (tile_changed) s.epoch[tile] = epoch;  // the next residual pass re-checks it and its neighbours
-        if (solve_count(sm.claim[0]) < s.refresh && !(ec & 16u)) atomicAdd(&s.flags[tile], kSolveOne);
+        if (solve_count(sm.claim[0]) < s.refresh && (capped || !(ec & 16u))) atomicAdd(&s.flags[tile], kSolveOne);
         learn_commit(s, tile, useful, wave, sweeps, sm.feat);
 #pragma unroll
         for (int e = 0; e < 4; ++e)
