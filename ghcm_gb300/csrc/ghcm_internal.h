@@ -29,7 +29,6 @@ enum : uint32_t {
     kEdgeMask = 0xFu << 4,
     kSolveOne = 1u << 8,   // bits 8-11: the tile's block-solves so far, counted up to Sched::refresh
     kSolveMask = 0xFu << 8,
-    kCapped   = 1u << 12,  // re-queued because its last block-solve hit the sweep cap
 };
 constexpr uint32_t kMaxRefresh = 15;  // largest Sched::refresh the 4-bit solve count holds
 constexpr uint32_t kDefaultRefresh = 1;

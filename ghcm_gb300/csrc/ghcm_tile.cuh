@@ -94,7 +94,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         // only a priority), while its data is staged, since the flag clear
         // acquires it.
         uint32_t const kold = atomicExch(&s.key[tile], inf_bits());
-        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask | kCapped));
+        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
         uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
         s_word[0] = f;
         s_word[1] = 0u;  // abort flag
@@ -199,14 +199,14 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     // (kUpdFresh: a value an earlier solve rounded low rises again and the
     // neighbours are told). Past fresh_sweeps sweeps, and for the reference
     // form, cells only fall (kUpdKeepMin); the limits end the one-ulp
-    // oscillations of nearly tied neighbours. A solve the sweep cap stopped
-    // spends the refresh budget and re-queues the tile with kCapped, whose
-    // next solve only lowers cells: otherwise a cap below fresh_sweeps could
-    // re-queue an oscillating tile forever.
-    int mode = (flags & kCapped) ? kUpdKeepMin
-                                 : (solve_count(flags) < s.refresh ? kUpdFresh
-                                                                   : (s.in_solve ? kUpdInSolve : kUpdKeepMin));
-    uint32_t const fresh_sweeps = 4u * B;
+    // oscillations of nearly tied neighbours. The last sweep before the sweep
+    // cap is always lower-only, so a solve the cap stops has lowered some cell
+    // by more than eps in that sweep: re-queues by the cap make progress and
+    // end (an oscillation that only ever returns to its start cannot hold a
+    // tile). A capped solve also spends the refresh budget.
+    int mode = solve_count(flags) < s.refresh ? kUpdFresh : (s.in_solve ? kUpdInSolve : kUpdKeepMin);
+    uint32_t const fresh_sweeps = min(4u * B, s.max_sweeps - 1u);
+    if (fresh_sweeps == 0u) mode = kUpdKeepMin;  // a cap of one sweep
     bool own_changed = false;
     bool capped = false;
     uint32_t sweeps = 0;
@@ -398,7 +398,7 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         if (tile_changed) s.epoch[tile] = epoch;  // the next residual pass re-checks it and its neighbours
         if (solve_count(flags) < s.refresh && (capped || !(s_word[4] & 16u))) atomicAdd(&s.flags[tile], kSolveOne);
         learn_commit(s, tile, useful, wave, sweeps, sm.feat);
-        if (capped) activate(s, tile, kFull | kCapped, m, nxt, s_krange);
+        if (capped) activate(s, tile, kFull, m, nxt, s_krange);
     }
     uint32_t const edge_changed = s_word[4];
     if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u) &&

@@ -58,7 +58,7 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     // Claim and stage.
     if (lane == 0) {
         uint32_t const kold = atomicExch(&s.key[tile], inf_bits());  // both in flight, as in solve_tile
-        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask | kCapped));
+        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
         uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
         sm.claim[0] = f;
         sm.claim[1] = kold;
@@ -123,10 +123,9 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     float const h_bot = sm.time[si<B>(x, B)];   // used by the last band
     float const eps = s.eps;
     // how sweeps bound the update (see solve_tile)
-    uint32_t const cf = sm.claim[0];
-    int mode = (cf & kCapped) ? kUpdKeepMin
-                              : (solve_count(cf) < s.refresh ? kUpdFresh : (s.in_solve ? kUpdInSolve : kUpdKeepMin));
-    uint32_t const fresh_sweeps = 4u * B;
+    int mode = solve_count(sm.claim[0]) < s.refresh ? kUpdFresh : (s.in_solve ? kUpdInSolve : kUpdKeepMin);
+    uint32_t const fresh_sweeps = min(4u * B, s.max_sweeps - 1u);  // see solve_tile
+    if (fresh_sweeps == 0u) mode = kUpdKeepMin;
     bool changed = false;
     bool capped = false;
     uint32_t sweeps = 0;
@@ -257,7 +256,7 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
             if (((imp_mask & ec) >> e) & 1u)
                 activate(s, static_cast<uint32_t>(neighbour_tile(I, tc.tx, tc.ty, e)), kEdgeBit0 << ((e + 2) & 3),
                          keys[e], nxt, s_krange);
-        if (capped) activate(s, tile, kFull | kCapped, lmin, nxt, s_krange);
+        if (capped) activate(s, tile, kFull, lmin, nxt, s_krange);
 #ifdef GHCM_PROFILE
         atomicAdd(&s.ctl->prof[3], static_cast<unsigned long long>(sweeps));
         atomicMax(&s.ctl->wave_max_sweeps, sweeps);

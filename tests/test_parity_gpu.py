@@ -313,18 +313,29 @@ def test_update_bounds_keep_parity(setups, medium, refresh, block, kernel):
         check_field(res.field, ref, seeds)
 
 
-@pytest.mark.parametrize("cap", [8, 16, 32])
+@pytest.mark.parametrize("cap", [4, 8, 16, 32])
 @pytest.mark.parametrize("kernel", [g.Kernel.Systolic, g.Kernel.FIM])
 @pytest.mark.parametrize("block", [8, 16])
 def test_sweep_caps_terminate_with_parity(setups, medium, cap, kernel, block):
     """Small inner-sweep caps (the autotuner tries B/2, B and 2B) re-queue
     capped tiles; the solve still ends, within a wave bound that turns a
     non-terminating schedule into GHCM_ERR_NOT_CONVERGED instead of a hang,
-    and keeps parity. (A cap of half the tile side leaves most solves capped,
-    and a capped tile's next solve only lowers cells, which drifts further
-    from the FIM; the caps here start at 8.)"""
+    and keeps parity."""
     for case in ("ring7_1024", "noise_1024"):
         speed, cost, seeds, ref = medium[case]
         s = setups(block, kernel, max_jobs=1024, max_sweeps=cap, max_waves=200000)
         res = g.eikonal_hcm_cuda_ex(s, speed, seeds, input_is_speed=True)
         check_field(res.field, ref, seeds)
+
+
+@pytest.mark.parametrize("kernel", [g.Kernel.Systolic, g.Kernel.FIM])
+@pytest.mark.parametrize("block", [8, 16])
+def test_one_sweep_cap_terminates(setups, oracle_lib, medium, kernel, block):
+    """A cap of one sweep (every solve lower-only and re-queued until nothing
+    moves) still ends at a fixed point, within the wave bound."""
+    speed, cost, seeds, ref = medium["noise_1024"]
+    s = setups(block, kernel, max_jobs=1024, max_sweeps=1, max_waves=200000)
+    res = g.eikonal_hcm_cuda_ex(s, speed, seeds, input_is_speed=True)
+    assert np.array_equal(np.isfinite(res.field), np.isfinite(ref))
+    assert oracle_lib.residual(cost, res.field) <= 1e-5
+    assert rel_diff(res.field, ref) <= 1e-4
