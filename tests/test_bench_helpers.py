@@ -24,7 +24,8 @@ def test_ring_traffic_comes_from_the_committed_capture():
     d = json.loads((PROFILES / "k_solve_ring7_4096.json").read_text())
     t = bench.load_traffic()
     assert t == d["dram_bytes_per_launch"] > 0
-    assert t == pytest.approx(d["dram_bytes_read"] + d["dram_bytes_write"], rel=1e-9)
+    if d.get("dram_bytes_read") is not None:
+        assert t == pytest.approx(d["dram_bytes_read"] + d["dram_bytes_write"], rel=1e-9)
     # a capture of another tile size or n is not used
     assert bench.load_traffic("k_solve_ring7_4096.json", block=32) is None
     assert bench.load_traffic("k_solve_ring7_4096.json", block=16, n=1024) is None
@@ -58,3 +59,10 @@ def test_fmm64_errors_conventions():
     e = bench.fmm64_errors(got, ref)
     assert e["linf"] == pytest.approx(0.5) and e["reachability_matches"]
     assert e["l1"] == pytest.approx(0.5 / 3)  # mean over the finite cells
+
+
+def test_headline_traffic_comes_from_the_committed_capture():
+    d = json.loads((PROFILES / "k_solve_noise4096_learned.json").read_text())
+    t = bench.load_traffic("k_solve_noise4096_learned.json")
+    assert t == pytest.approx(d["dram_bytes_read"] + d["dram_bytes_write"]) and t > 0
+    assert d["block_solves"] > 0
