@@ -29,22 +29,38 @@ namespace ghcm {
 //   9 log2(1 + solves so far) / 8
 //  10 re-queued in full (residual check or sweep cap)
 //  11 edges with new boundary values / 4
-// key/kmax: the tile's activation keys (float), flags: its scheduler flags.
-__device__ __forceinline__ void tile_features(const Sched& s, uint32_t tile, uint32_t flags, float key, float kmax,
-                                              uint32_t wave, float front, float span, float (&f)[kFeatures]) {
-    const Learn& L = s.learn;
+//
+// The features from the loaded tile state. key/kmax: the tile's activation
+// keys, flags: its scheduler flags, tm: smallest time, ns: solves so far,
+// st: log speed statistics, lc: wave of its last useful solve + 1, act:
+// active neighbours, front/span: this wave's key range.
+__device__ __forceinline__ void features_from(float key, float kmax, uint32_t flags, float tm, uint32_t ns, float4 st,
+                                              uint32_t lc, int act, uint32_t wave, float front, float span,
+                                              float (&f)[kFeatures]) {
     float const inv = 1.0f / span;
     float const k = (key < f_inf()) ? key : front + span;
     f[0] = fminf(fmaxf((k - front) * inv, 0.f), 1.f);
     f[1] = fminf(fmaxf((fmaxf(kmax, k) - k) * inv, 0.f), 1.f);
-    float const tm = __ldcg(&s.tmin[tile]);
-    uint32_t const ns = __ldcg(&L.nsolve[tile]);
     f[2] = ns ? 0.f : 1.f;
     f[3] = (tm < f_inf()) ? fminf(fmaxf((tm - k) * inv, -1.f), 1.f) : 1.f;
-    float4 const st = __ldg(&L.tstat[tile]);
     f[4] = st.x;
     f[5] = st.y;
     f[6] = st.z;
+    f[7] = 0.25f * static_cast<float>(act);
+    f[8] = lc ? fminf(static_cast<float>(wave + 1u - lc), 64.f) * (1.f / 64.f) : 1.f;
+    f[9] = log2f(1.f + static_cast<float>(ns)) * 0.125f;
+    f[10] = (flags & kFull) ? 1.f : 0.f;
+    f[11] = 0.25f * static_cast<float>(__popc((flags & kEdgeMask) >> 4));
+}
+
+// Loads a tile's state and computes its features (claim-time trace and veto).
+__device__ __forceinline__ void tile_features(const Sched& s, uint32_t tile, uint32_t flags, float key, float kmax,
+                                              uint32_t wave, float front, float span, float (&f)[kFeatures]) {
+    const Learn& L = s.learn;
+    float const tm = __ldcg(&s.tmin[tile]);
+    uint32_t const ns = __ldcg(&L.nsolve[tile]);
+    float4 const st = __ldg(&L.tstat[tile]);
+    uint32_t const lc = __ldcg(&L.last_change[tile]);
     const Inst& I = s.insts[inst_of(s, tile)];
     uint32_t const local = tile - I.tile_base;
     uint32_t const tx = local % I.tiles_x, ty = local / I.tiles_x;
@@ -52,14 +68,9 @@ __device__ __forceinline__ void tile_features(const Sched& s, uint32_t tile, uin
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
         int const nb = neighbour_tile(I, tx, ty, e);
-        if (nb >= 0 && (ld_relaxed(&s.flags[nb]) & kActive)) ++act;
+        if (nb >= 0 && (__ldcg(&s.flags[nb]) & kActive)) ++act;
     }
-    f[7] = 0.25f * static_cast<float>(act);
-    uint32_t const lc = __ldcg(&L.last_change[tile]);
-    f[8] = lc ? fminf(static_cast<float>(wave + 1u - lc), 64.f) * (1.f / 64.f) : 1.f;
-    f[9] = log2f(1.f + static_cast<float>(ns)) * 0.125f;
-    f[10] = (flags & kFull) ? 1.f : 0.f;
-    f[11] = 0.25f * static_cast<float>(__popc((flags & kEdgeMask) >> 4));
+    features_from(key, kmax, flags, tm, ns, st, lc, act, wave, front, span, f);
 }
 
 // The MLP parameters staged in the kernel's dynamic shared memory (kParams
@@ -135,20 +146,38 @@ __device__ void tile_speed_stats(const Sched& s, uint32_t tile) {
     }
 }
 
-// Score policy: the model logit of `tile`, just appended at entry `pos` of
-// list[nxt] by the calling CTA's solve, computed by the calling warp and kept
-// in that entry's score for the next decision. Tiles re-queued in full need
-// none (they are always taken).
-__device__ void score_queued_warp(const Sched& s, uint32_t tile, uint32_t nxt, uint32_t pos, uint32_t wave) {
-    uint32_t const flags = ld_relaxed(&s.flags[tile]);
-    if (flags & kFull) return;
-    Ctl* ctl = s.ctl;
+// Score policy: the model logit of `tile` (tile (tx, ty) of instance I),
+// just appended at entry `pos` of list[nxt] by the calling CTA's solve,
+// computed by the calling warp and kept in that entry's score for the next
+// decision. Every load is issued at once (one round trip; the neighbours'
+// ids come from the coordinates, not from memory). Tiles re-queued in full
+// need no score (they are always taken).
+__device__ void score_queued_warp(const Sched& s, const Inst& I, uint32_t tile, uint32_t tx, uint32_t ty,
+                                  uint32_t nxt, uint32_t pos, uint32_t wave) {
+    const Learn& L = s.learn;
+    uint32_t const flags = __ldcg(&s.flags[tile]);
     float const key = __uint_as_float(__ldcg(&s.key[tile]));
-    float const kmax = __uint_as_float(__ldcg(&s.learn.kmax[tile]));
+    float const kmax = __uint_as_float(__ldcg(&L.kmax[tile]));
+    float const tm = __ldcg(&s.tmin[tile]);
+    uint32_t const ns = __ldcg(&L.nsolve[tile]);
+    float4 const st = __ldg(&L.tstat[tile]);
+    uint32_t const lc = __ldcg(&L.last_change[tile]);
+    float const front = __ldcg(&s.ctl->wave_front);
+    float const span = __ldcg(&s.ctl->wave_span);
+    uint32_t nf[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        int const nb = neighbour_tile(I, tx, ty, e);
+        nf[e] = nb >= 0 ? __ldcg(&s.flags[nb]) : 0u;
+    }
+    if (flags & kFull) return;
+    int act = 0;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) act += (nf[e] & kActive) ? 1 : 0;
     float x[kFeatures];
-    tile_features(s, tile, flags, key, kmax, wave, ld_relaxed_f(&ctl->wave_front), ld_relaxed_f(&ctl->wave_span), x);
+    features_from(key, kmax, flags, tm, ns, st, lc, act, wave, front, span, x);
     float const z = mlp_logit_warp(g_mlp_params, x);
-    if ((threadIdx.x & 31) == 0) __stcg(&s.learn.lscore[nxt][pos], z);
+    if ((threadIdx.x & 31) == 0) __stcg(&L.lscore[nxt][pos], z);
 }
 
 }  // namespace ghcm

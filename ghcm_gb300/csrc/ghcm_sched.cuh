@@ -118,17 +118,29 @@ __device__ __forceinline__ uint32_t tile_key(const Sched& s, uint32_t tile) {
     return __float_as_uint(k);
 }
 
-// Selects the n smallest keys among the m (> n) tiles of `list`, by the whole
-// CTA: a histogram of SELECT_BINS bins over [lo, hi] (the keys' range, or a
+// Score gate of the learned schedule for select_top_n: tiles whose score (at
+// their list entry) reaches `thr` go first, at most `cap` of them; the wave
+// is filled up to the select's n in key order.
+struct ScoreGate {
+    bool on;
+    float thr;     // threshold logit
+    uint32_t cap;  // most jobs a wave
+};
+
+// Selects the n smallest keys among the m tiles of list[L], by the whole CTA:
+// a histogram of SELECT_BINS bins over [lo, hi] (the keys' range, or a
 // superset of it; with have_range false a first pass finds it), a scan for
 // the bin holding the n-th key, then every tile of a lower bin and enough
-// tiles of that bin (in list order) go to s.jobs, the rest to `carry`. The
-// order is exact up to 1/SELECT_BINS of the range. Returns the number carried.
+// tiles of that bin (in list order) go to s.jobs from jobs_base, the rest to
+// list[L ^ 1]. The order is exact up to 1/SELECT_BINS of the range. With the
+// gate on, bin 0 holds the qualifying tiles and the keys use the others; n
+// becomes max(min(qualifying, cap), n). Returns the number carried; the
+// jobs are m - carried.
 constexpr int SELECT_BINS = 2048;
 
 template <int THREADS, int CACHE>
 __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_t n, uint32_t* s_hist, uint32_t* s_sel,
-                                 float lo, float hi, bool have_range, uint32_t jobs_base) {
+                                 float lo, float hi, bool have_range, uint32_t jobs_base, ScoreGate gate) {
     __shared__ float s_fmin[THREADS / 32], s_fmax[THREADS / 32];
     int const tid = threadIdx.x;
     int const lane = tid & 31, warp = tid >> 5;
@@ -167,19 +179,22 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
     } else {
         __syncthreads();
     }
+    int const first = gate.on ? 1 : 0;  // bins of the keys: [first, SELECT_BINS)
     float const span = hi - lo;
-    float const scale = (span > 0.f) ? static_cast<float>(SELECT_BINS - 1) / span : 0.f;
-    auto bin_of = [&](float k) -> int {
+    float const scale = (span > 0.f) ? static_cast<float>(SELECT_BINS - 1 - first) / span : 0.f;
+    auto bin_of = [&](uint32_t i, uint32_t t) -> int {
+        if (gate.on && __ldcg(&score[i]) >= gate.thr) return 0;  // +inf for tiles re-queued in full
+        float const k = __uint_as_float(tile_key(s, t));
         if (!(k < f_inf())) return SELECT_BINS - 1;
-        int const b = static_cast<int>((k - lo) * scale);
-        return b < 0 ? 0 : (b >= SELECT_BINS ? SELECT_BINS - 1 : b);
+        int const b = first + static_cast<int>((k - lo) * scale);
+        return b < first ? first : (b >= SELECT_BINS ? SELECT_BINS - 1 : b);
     };
     // pass 2: histogram. Up to CACHE entries per thread (a register budget set
-    // by the kernel) keep their key in registers for the gather pass (lists
+    // by the kernel) keep their bin in registers for the gather pass (lists
     // of up to THREADS * CACHE tiles), so it re-reads only the coalesced list;
-    // longer lists load keys again there.
+    // longer lists find bins again there.
     bool const cached = m <= static_cast<uint32_t>(THREADS * CACHE);
-    uint32_t ck[CACHE];
+    int cb[CACHE];
     if (cached) {
         uint32_t ct[CACHE];
 #pragma unroll
@@ -188,66 +203,73 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
             ct[u] = (i < m) ? __ldcg(&list[i]) : 0u;
         }
 #pragma unroll
-        for (int u = 0; u < CACHE; ++u)
-            ck[u] = (tid + u * THREADS < m) ? tile_key(s, ct[u]) : 0u;
+        for (int u = 0; u < CACHE; ++u) {
+            uint32_t const i = tid + u * THREADS;
+            cb[u] = (i < m) ? bin_of(i, ct[u]) : 0;
+        }
 #pragma unroll
         for (int u = 0; u < CACHE; ++u)
-            if (tid + u * THREADS < m) atomicAdd(&s_hist[bin_of(__uint_as_float(ck[u]))], 1u);
+            if (tid + u * THREADS < m) atomicAdd(&s_hist[cb[u]], 1u);
     } else {
         uint32_t i = tid;
         for (; i + 3u * THREADS < m; i += 4u * THREADS) {
             uint32_t t4[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) t4[u] = __ldcg(&list[i + u * THREADS]);
-            uint32_t k4[4];
+            int b4[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) k4[u] = tile_key(s, t4[u]);
+            for (int u = 0; u < 4; ++u) b4[u] = bin_of(i + u * THREADS, t4[u]);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) atomicAdd(&s_hist[bin_of(__uint_as_float(k4[u]))], 1u);
+            for (int u = 0; u < 4; ++u) atomicAdd(&s_hist[b4[u]], 1u);
         }
-        for (; i < m; i += THREADS) atomicAdd(&s_hist[bin_of(__uint_as_float(tile_key(s, __ldcg(&list[i]))))], 1u);
+        for (; i < m; i += THREADS) atomicAdd(&s_hist[bin_of(i, __ldcg(&list[i]))], 1u);
     }
     __syncthreads();
-    // the bin holding the n-th smallest key: thread t scans bins [t*PER, (t+1)*PER)
-    constexpr int PER = SELECT_BINS / THREADS;
-    uint32_t part = 0u;
-#pragma unroll
-    for (int j = 0; j < PER; ++j) part += s_hist[tid * PER + j];
-    uint32_t incl = part;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t const v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    __shared__ uint32_t s_wsum[THREADS / 32];
-    if (lane == 31) s_wsum[warp] = incl;
-    __syncthreads();
-    uint32_t wbase = 0u;
-    for (int w = 0; w < warp; ++w) wbase += s_wsum[w];
-    uint32_t below = wbase + incl - part;
-    if (below < n && n <= below + part) {
-#pragma unroll
-        for (int j = 0; j < PER; ++j) {
-            uint32_t const h = s_hist[tid * PER + j];
-            if (below + h >= n) {
-                s_sel[0] = static_cast<uint32_t>(tid * PER + j);
-                s_sel[1] = n - below;  // how many of the boundary bin to take
-                break;
-            }
-            below += h;
-        }
-    }
+    if (gate.on) n = max(min(s_hist[0], gate.cap), n);  // qualifying tiles first, up to the cap
     if (tid == 0) {
+        s_sel[0] = SELECT_BINS;  // n >= m: every bin lies below the boundary
+        s_sel[1] = 0u;
         s_sel[2] = 0u;
         s_sel[3] = 0u;
         s_sel[4] = 0u;
     }
     __syncthreads();
+    if (n < m) {
+        // the bin holding the n-th smallest entry: thread t scans bins [t*PER, (t+1)*PER)
+        constexpr int PER = SELECT_BINS / THREADS;
+        uint32_t part = 0u;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) part += s_hist[tid * PER + j];
+        uint32_t incl = part;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t const v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        __shared__ uint32_t s_wsum[THREADS / 32];
+        if (lane == 31) s_wsum[warp] = incl;
+        __syncthreads();
+        uint32_t wbase = 0u;
+        for (int w = 0; w < warp; ++w) wbase += s_wsum[w];
+        uint32_t below = wbase + incl - part;
+        if (below < n && n <= below + part) {
+#pragma unroll
+            for (int j = 0; j < PER; ++j) {
+                uint32_t const h = s_hist[tid * PER + j];
+                if (below + h >= n) {
+                    s_sel[0] = static_cast<uint32_t>(tid * PER + j);
+                    s_sel[1] = n - below;  // how many of the boundary bin to take
+                    break;
+                }
+                below += h;
+            }
+        }
+        __syncthreads();
+    }
     int const bnd = static_cast<int>(s_sel[0]);
     uint32_t const take_eq = s_sel[1];
     // pass 3: gather; a carried entry keeps its learned score
-    auto place = [&](uint32_t i, uint32_t t, uint32_t kb) {
-        int const b = bin_of(__uint_as_float(kb));
+    auto place = [&](uint32_t i, uint32_t t, int b) {
         bool take = b < bnd;
         if (!take && b == bnd) take = atomicAdd(&s_sel[2], 1u) < take_eq;
         if (take) {
@@ -265,24 +287,26 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
 #pragma unroll
         for (int u = 0; u < CACHE; ++u) {
             uint32_t const i = tid + u * THREADS;
-            if (i < m) place(i, __ldcg(&list[i]), ck[u]);
+            if (i < m) place(i, __ldcg(&list[i]), cb[u]);
         }
     } else {
         uint32_t i = tid;
         for (; i + 3u * THREADS < m; i += 4u * THREADS) {  // four entries in flight per thread
-            uint32_t t4[4], k4[4];
+            uint32_t t4[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) t4[u] = __ldcg(&list[i + u * THREADS]);
+            int b4[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) k4[u] = tile_key(s, t4[u]);
+            for (int u = 0; u < 4; ++u) b4[u] = bin_of(i + u * THREADS, t4[u]);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) place(i + u * THREADS, t4[u], k4[u]);
+            for (int u = 0; u < 4; ++u) place(i + u * THREADS, t4[u], b4[u]);
         }
         for (; i < m; i += THREADS) {
             uint32_t const t = __ldcg(&list[i]);
-            place(i, t, tile_key(s, t));
+            place(i, t, bin_of(i, t));
         }
     }
+    if (gate.on && tid == 0) s_sel[5] = s_hist[0];  // qualifying tiles, for the counters
     __syncthreads();
     return s_sel[4];
 }
@@ -329,20 +353,29 @@ __device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned l
 
 __device__ __forceinline__ float ld_relaxed_f(const float* p) { return __uint_as_float(ld_relaxed(reinterpret_cast<const uint32_t*>(p))); }
 
-// Runs the plain top-n on list[L] (m tiles): its n lowest keys become jobs
-// base.. of the next JOBS phase (or, with no jobs before them and m <= n, the
-// list itself), the rest is carried to list[L ^ 1], where the activations of
-// that phase also go. Returns {in_list, job count} in s_sel[8], [11].
+// Runs the top-n on list[L] (m tiles): its n lowest keys (with the gate on,
+// the qualifying tiles first, see ScoreGate) become jobs base.. of the next
+// JOBS phase (or, with no jobs before them and m <= n, the list itself), the
+// rest is carried to list[L ^ 1], where the activations of that phase also
+// go. Returns {in_list, job count} in s_sel[8], [11].
 template <int THREADS, int CACHE>
-__device__ void plan_plain_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t n, uint32_t base, float lo, float hi,
-                                uint32_t* s_hist, uint32_t* s_sel) {
+__device__ void plan_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t n, uint32_t base, float lo, float hi,
+                          uint32_t* s_hist, uint32_t* s_sel, ScoreGate gate) {
     Ctl* ctl = s.ctl;
     bool const all = m <= n;
     uint32_t carried = 0u;
+    uint32_t qualifying = 0u;  // learned schedule: tiles scoring at or above the threshold
     if (!all) {
-        carried = select_top_n<THREADS, CACHE>(s, L, m, n, s_hist, s_sel, lo, hi, s.key_mode == 0u, base);
-    } else if (base) {
-        for (uint32_t i = threadIdx.x; i < m; i += THREADS) s.jobs[base + i] = __ldcg(&s.list[L][i]);
+        carried = select_top_n<THREADS, CACHE>(s, L, m, n, s_hist, s_sel, lo, hi, s.key_mode == 0u, base, gate);
+        if (gate.on) qualifying = s_sel[5];
+    } else {
+        if (base)
+            for (uint32_t i = threadIdx.x; i < m; i += THREADS) s.jobs[base + i] = __ldcg(&s.list[L][i]);
+        if (gate.on) {
+            bool q = false;
+            for (uint32_t i = threadIdx.x; i < m; i += THREADS) q |= __ldcg(&s.learn.lscore[L][i]) >= gate.thr;
+            qualifying = __syncthreads_or(q) ? 1u : 0u;
+        }
     }
     if (threadIdx.x == 0) {
         ctl->count[L ^ 1u] = carried;
@@ -351,80 +384,9 @@ __device__ void plan_plain_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t
         ctl->krange[L ^ 1u][1] = carried ? __float_as_uint(hi) : 0u;
         s_sel[8] = (all && base == 0u) ? 1u : 0u;
         s_sel[11] = base + (all ? m : m - carried);
+        // learned schedule: a wave that took tiles by score, or one that went by key alone
+        if (gate.on) atomicAdd(qualifying ? &ctl->score_waves : &ctl->fallback_waves, 1u);
     }
-}
-
-// Learned schedule, score policy: the tiles of list[act] (m) re-queued in full
-// or whose score (written at their list entry when they were queued) reaches
-// the threshold become jobs (at most max_jobs), the rest are carried to
-// list[act ^ 1]; if fewer
-// than fallback_jobs were taken the wave is filled from the carried tiles in
-// plain key order. Returns the list the JOBS phase treats as current (its
-// activations go to the other one). Counters and s_sel[8], [11] as in
-// plan_plain_jobs.
-template <int THREADS, int CACHE>
-__device__ uint32_t plan_learned_jobs(const Sched& s, uint32_t act, uint32_t m, float lo, float hi, uint32_t* s_hist,
-                                      uint32_t* s_sel) {
-    Ctl* ctl = s.ctl;
-    int const tid = threadIdx.x;
-    float const thr = logf(s.learn.threshold / (1.f - s.learn.threshold));
-    uint32_t const cap = s.max_jobs;
-    if (tid == 0) {
-        s_sel[6] = 0u;  // taken
-        s_sel[7] = 0u;  // carried
-    }
-    __syncthreads();
-    const uint32_t* list = s.list[act];
-    const float* score = s.learn.lscore[act];
-    // a carried entry keeps its score
-    auto place = [&](uint32_t i, uint32_t t, float z) {
-        bool take = z >= thr;  // +inf for tiles re-queued in full
-        if (take) {
-            uint32_t const pos = atomicAdd(&s_sel[6], 1u);
-            if (pos < cap)
-                s.jobs[pos] = t;
-            else
-                take = false;
-        }
-        if (!take) {
-            uint32_t const pos = atomicAdd(&s_sel[7], 1u);
-            s.list[act ^ 1u][pos] = t;
-            s.learn.lscore[act ^ 1u][pos] = z;
-        }
-    };
-    // ids and scores are coalesced loads of the list
-    uint32_t i = tid;
-    for (; i + 3u * THREADS < m; i += 4u * THREADS) {  // four entries in flight per thread
-        uint32_t t4[4];
-        float z4[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            t4[u] = __ldcg(&list[i + u * THREADS]);
-            z4[u] = __ldcg(&score[i + u * THREADS]);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) place(i + u * THREADS, t4[u], z4[u]);
-    }
-    for (; i < m; i += THREADS) place(i, __ldcg(&list[i]), __ldcg(&score[i]));
-    __syncthreads();
-    uint32_t const take = min(s_sel[6], cap);
-    uint32_t const carried = s_sel[7];
-    uint32_t const want = min(s.learn.fallback_jobs, cap);
-    __syncthreads();  // s_sel[6..7] are read before the select reuses s_sel
-    if (take >= want || carried == 0u) {
-        if (tid == 0) {
-            ctl->count[act ^ 1u] = carried;
-            ctl->krange[act ^ 1u][0] = carried ? __float_as_uint(lo) : inf_bits();
-            ctl->krange[act ^ 1u][1] = carried ? __float_as_uint(hi) : 0u;
-            s_sel[8] = 0u;
-            s_sel[11] = take;
-            atomicAdd(take ? &ctl->score_waves : &ctl->fallback_waves, 1u);
-        }
-        return act;
-    }
-    plan_plain_jobs<THREADS, CACHE>(s, act ^ 1u, carried, want - take, take, lo, hi, s_hist, s_sel);
-    if (tid == 0) atomicAdd(take ? &ctl->score_waves : &ctl->fallback_waves, 1u);
-    return act ^ 1u;
 }
 
 // Decides the next phase; run by the whole of the last CTA to reach the wave
@@ -492,10 +454,14 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
 #ifdef GHCM_PROFILE
             uint64_t const p_sel0 = global_ns();
 #endif
-            if (s.learn.params && !s.learn.veto)
-                ncur = plan_learned_jobs<THREADS, CACHE>(s, act, m, lo, hi, s_hist, s_sel);
-            else
-                plan_plain_jobs<THREADS, CACHE>(s, act, m, s.max_jobs, 0u, lo, hi, s_hist, s_sel);
+            // learned schedule, score policy: the tiles scoring at or above the
+            // threshold (at list entries, written when they were queued) first,
+            // up to max_jobs, filled to fallback_jobs in plain key order
+            bool const scored = s.learn.params && !s.learn.veto;
+            ScoreGate gate{scored, 0.f, s.max_jobs};
+            if (scored) gate.thr = logf(s.learn.threshold / (1.f - s.learn.threshold));
+            uint32_t const n = scored ? min(s.learn.fallback_jobs, s.max_jobs) : s.max_jobs;
+            plan_jobs<THREADS, CACHE>(s, act, m, n, 0u, lo, hi, s_hist, s_sel, gate);
             if (tid == 0) atomicAdd(&ctl->waves, 1u);
 #ifdef GHCM_PROFILE
             if (tid == 0) {  // [20] decision loads, [21] job planning, [22] waves that ran the top-n select
