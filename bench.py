@@ -8,10 +8,11 @@ fractal value-noise speed field (6 octaves, base period 512, persistence 0.5,
 speed = clamp(exp(2 noise), 0.02, 1)) with 16 sources, seed 1, h = 1, tiles of
 16, eps = 1e-5, solved by the LEARNED block schedule (the 12-64-64-1 MLP of
 ghcm_gb300/models/, trained on traces of the plain solver on 32 other seeds;
-score policy, at most 4096 jobs a wave, filled to 1024 in key order). `value`
-is its Mcell/s; the PLAIN device schedule (n = 1024) is timed the same way in
-the same run and reported beside it (`plain`, `learned_vs_plain`), with the
-other plain n and the veto policy under `others`. Both fields are checked
+score policy, at most 4096 jobs a wave, filled to 4 x SMs in key order).
+`value` is its Mcell/s; the PLAIN device schedule is timed the same way in
+the same run at n = 4 x SMs, 1024, 2048 and 4096, and the fastest is reported
+beside it (`plain`, `learned_vs_plain`), the others and the veto policy under
+`others`. Both fields are checked
 against the reference's CPU FIM and FMM (oracle restatements, bit-exact to the
 reference build) and an FP64 FMM. Sub-objects: `ring_4096` - the 4096 x 4096
 seven-ring field (radii 256..1920, barrier width 16, speed 0.01, 64-cell gaps,
@@ -69,9 +70,9 @@ LAUNCHES_PER_LEARNED_SOLVE = 4  # the same and k_tile_stats (the learned feature
 BLOCK = 16
 N_JOBS = 256  # the seven-ring workload's headline n
 N_SWEEP = (256, 1024, 4096)
-LEARNED_CAPS = {"max_jobs": 4096, "fallback_jobs": 1024}  # the learned schedule's jobs per wave: cap, plain fill
-PLAIN_N = 1024  # the plain schedule the learned one is compared with (the fastest n on this field)
-PLAIN_SWEEP = (512, 1024, 2048, 4096)
+LEARNED_CAP = 4096  # the learned schedule's most jobs a wave; waves are filled to 4 x SMs in key order
+PLAIN_SWEEP = (0, 1024, 2048, 4096)  # plain n timed beside it (0: 4 x SMs, one job per CTA of the 4-CTA grid);
+                                     # the fastest is the comparison
 EPS = 1e-5
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB of L2
 
@@ -904,12 +905,13 @@ def run_ring(args, world, rank, local) -> int:
 
 def run_noise(args, world, rank, local) -> int:
     """The headline: the learned block schedule against the plain one on the
-    4096^2 noise field. `value` is the learned schedule's Mcell/s; the plain
-    schedule (n = PLAIN_N, the fastest plain n on this field) is timed the
-    same way in the same run beside it, with the other plain n and the veto
-    policy; both fields are checked against the reference FIM and FMM and the
-    FP64 FMM. The seven-ring field (C2) and the 256^2 ring (C1) ride along as
-    sub-objects."""
+    4096^2 noise field. `value` is the learned schedule's Mcell/s (at most
+    LEARNED_CAP jobs a wave, filled to 4 x SMs in key order); the plain
+    schedule is timed the same way in the same run at each n of PLAIN_SWEEP
+    and the fastest is the comparison (`plain`), the others and the veto
+    policy under `others`; both fields are checked against the reference FIM
+    and FMM and the FP64 FMM. The seven-ring field (C2) and the 256^2 ring
+    (C1) ride along as sub-objects."""
     import torch
 
     import ghcm_gb300 as g
@@ -938,12 +940,18 @@ def run_noise(args, world, rank, local) -> int:
     d_time_p = torch.empty_like(d_speed)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
-    s_learned = _learned_setup(g, learned, params, threshold, learned.POLICY_SCORE, **LEARNED_CAPS)
-    s_plain = g.HcmSetup(g.HcmConfig(block_size=BLOCK, max_jobs=PLAIN_N, fim_minimum_change=EPS))
+    with g.HcmSetup(g.HcmConfig(block_size=BLOCK)) as probe:
+        sms = probe.sm_count
+    fill = 4 * sms
+    caps = {"max_jobs": LEARNED_CAP, "fallback_jobs": fill}
+    s_learned = _learned_setup(g, learned, params, threshold, learned.POLICY_SCORE, **caps)
+    plain_ns = [n or fill for n in (PLAIN_SWEEP if not args.quick else (0,))]
+    s_plains = {n: g.HcmSetup(g.HcmConfig(block_size=BLOCK, max_jobs=n, fim_minimum_change=EPS)) for n in plain_ns}
 
     for _ in range(args.warmup):
         g.solve_device(s_learned, d_speed, d_seeds, d_time_l, stream=stream)
-        g.solve_device(s_plain, d_speed, d_seeds, d_time_p, stream=stream)
+        for sp in s_plains.values():
+            g.solve_device(sp, d_speed, d_seeds, d_time_p, stream=stream)
     barrier()
 
     def timed(setup, d_time):
@@ -962,8 +970,11 @@ def run_noise(args, world, rank, local) -> int:
         t_wall = time.perf_counter()
         step_ms, stats = timed(s_learned, d_time_l)
         t_wall = time.perf_counter() - t_wall
-        plain_ms, plain_stats = timed(s_plain, d_time_p)
+        plain_runs = {n: timed(sp, d_time_p) for n, sp in s_plains.items()}
     clocks = clk.summary()
+    plain_n = min(plain_runs, key=lambda n: sum(plain_runs[n][0]))  # the fastest plain n is the comparison
+    plain_ms, plain_stats = plain_runs[plain_n]
+    s_plain = s_plains[plain_n]
     ms = sum(step_ms) / len(step_ms)
     pms = sum(plain_ms) / len(plain_ms)
     if dist is not None:
@@ -999,25 +1010,21 @@ def run_noise(args, world, rank, local) -> int:
     field_l = d_time_l.cpu().numpy()
     field_p = d_time_p.cpu().numpy()
 
-    # the plain schedule's other n and the veto policy, device-timed (fewer steps)
+    # the plain schedule's other n (timed above) and the veto policy, device-timed (fewer steps)
     k = max(1, min(args.steps, 3))
     others, other_fields = {}, {}
-    for n in PLAIN_SWEEP:
-        if n == PLAIN_N or args.quick:
+    for n, (n_ms, n_st) in plain_runs.items():
+        if n == plain_n:
             continue
-        with g.HcmSetup(g.HcmConfig(block_size=BLOCK, max_jobs=n, fim_minimum_change=EPS)) as s:
-            d_t = torch.empty_like(d_speed)
-            o_ms, o_st = timed_device_solves(g, s, d_speed, d_seeds, d_t, stream, flush, k, 1)
-        other_fields[f"plain_n{n}"] = d_t.cpu().numpy()
-        others[f"plain_n{n}"] = {"mcells": cells / (o_ms * 1e3), "ms": o_ms,
-                                 "block_solves": statistics.mean(x["block_solves"] for x in o_st),
-                                 "waves": statistics.mean(x["waves"] for x in o_st)}
+        others[f"plain_n{n}"] = {"mcells": cells / (statistics.mean(n_ms) * 1e3), "ms": statistics.mean(n_ms),
+                                 "block_solves": statistics.mean(x["block_solves"] for x in n_st),
+                                 "waves": statistics.mean(x["waves"] for x in n_st)}
     if not args.quick:
-        s_veto = _learned_setup(g, learned, params, threshold, learned.POLICY_VETO, max_jobs=PLAIN_N)
+        s_veto = _learned_setup(g, learned, params, threshold, learned.POLICY_VETO, max_jobs=plain_n)
         d_t = torch.empty_like(d_speed)
         o_ms, o_st = timed_device_solves(g, s_veto, d_speed, d_seeds, d_t, stream, flush, k, 1)
-        other_fields["learned_veto_n1024"] = d_t.cpu().numpy()
-        others["learned_veto_n1024"] = {"mcells": cells / (o_ms * 1e3), "ms": o_ms,
+        other_fields["learned_veto"] = d_t.cpu().numpy()
+        others["learned_veto"] = {"n": plain_n, "mcells": cells / (o_ms * 1e3), "ms": o_ms,
                                         "block_solves": statistics.mean(x["block_solves"] for x in o_st),
                                         "waves": statistics.mean(x["waves"] for x in o_st)}
         s_veto.close()
@@ -1034,12 +1041,13 @@ def run_noise(args, world, rank, local) -> int:
         "warmup": args.warmup, "ms_per_step": ms,
         "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "schedule": "learned (score policy)", "block": BLOCK, **LEARNED_CAPS,
+        "config": {"workload": WORKLOAD, "schedule": "learned (score policy)", "block": BLOCK, **caps,
                    "model": MODEL.name, "model_train_seeds": int(len(meta.get("train_seeds", []))),
                    "threshold": threshold, "field_seed": NOISE_EVAL_SEED, "sources": int(len(seeds)), "eps": EPS,
                    "l2": "flushed between steps (256 MiB write outside the events)",
                    "parallelism": f"replicas x{world}"},
-        "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": pms, "n": PLAIN_N,
+        "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": pms, "n": plain_n,
+                  "chosen_as": f"fastest of plain n in {sorted(plain_runs)}",
                   "block_solves": plain_solves, "waves": statistics.mean(st["waves"] for st in plain_stats),
                   "kernel_ms": statistics.mean(st["kernel_ms"] for st in plain_stats),
                   "e2e": None if args.quick else {"value": world * cells / (e2e_plain_ms * 1e3), "unit": UNIT,
@@ -1083,7 +1091,7 @@ def run_noise(args, world, rank, local) -> int:
             for name, f in other_fields.items():
                 others[name]["max_rel_vs_fim"] = rel_diff(f, fim)
             if not args.quick:
-                line["reference_schedule_n1024"] = reference_schedule(o, cost, seeds, BLOCK, PLAIN_N, 256, fim)
+                line["reference_schedule_n1024"] = reference_schedule(o, cost, seeds, BLOCK, 1024, 256, fim)
         if not args.quick:
             line["ring_4096"] = ring_4096(g, dev, stream, flush, k, 1, checks=not args.no_cpu_baseline)
         if not args.no_cpu_baseline and not args.quick:
@@ -1092,7 +1100,8 @@ def run_noise(args, world, rank, local) -> int:
             line["kernels"] = kernel_compare(g, dev, stream, flush, k)
         print(json.dumps(line), flush=True)
     s_learned.close()
-    s_plain.close()
+    for sp in s_plains.values():
+        sp.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0
