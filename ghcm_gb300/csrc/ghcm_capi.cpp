@@ -167,10 +167,13 @@ int run_solve(ghcm_ctx* ctx, const float* d_field, int input_is_speed, uint32_t 
     cudaEventRecord(ctx->ev0, st);
     if ((e = launch_init(s, 1, static_cast<uint64_t>(w) * h, n_seeds, static_cast<int>(B), ctx->sms, st)) != cudaSuccess)
         return map_cuda(e);
-    // the wide build for plain waves of many jobs; the learned schedule stays on
-    // the 4-CTA build, where its scoring ran 7.2 ms against 9.0 ms on the wide
-    // one (4096^2 noise, max_jobs 4096)
-    bool const wide = !learned && wide_for(ctx->launch, ctx->sms, s.max_jobs) && ctx->wide.blocks_per_sm > 0;
+    // the wide build for waves of many jobs. A learned schedule's waves hold
+    // at least its fill (fallback_jobs) and up to max_jobs: it goes wide only
+    // when the fill alone is that large (on the 4096^2 noise field, cap 4096
+    // and fill 1024, its scoring ran 7.2 ms on the 4-CTA build against 9.0 ms
+    // on the wide one)
+    uint32_t const wide_jobs = learned ? s.learn.fallback_jobs : s.max_jobs;
+    bool const wide = wide_for(ctx->launch, ctx->sms, wide_jobs) && ctx->wide.blocks_per_sm > 0;
     LaunchInfo const& li = wide ? ctx->wide : ctx->launch;
     int const grid = persistent_grid(li, ctx->sms, s.max_jobs);
     cudaEventRecord(ctx->ev2, st);

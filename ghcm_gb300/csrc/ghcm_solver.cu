@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, CTAS) k_solve(const __gr
                     break;
                 }
                 int const r = solve_tile<B, FIM>(s, job, cur ^ 1u, sm, &s_bar, parity, tma_pending, s_word, s_red,
-                                                 s_krange, wave, s_state[kStResid] + 1u, nj);
+                                                 s_krange, wave, s_state[kStResid] + 1u);
                 if (r == kJobFailed) break;
                 solves += (r == kJobSolved) ? 1u : 0u;
             }

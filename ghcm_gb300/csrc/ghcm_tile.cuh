@@ -75,7 +75,7 @@ enum : int { kJobFailed = 0, kJobSolved = 1, kJobDeferred = 2 };
 template <int B, bool FIM>
 __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<B>& sm, uint64_t* bar,
                            uint32_t& parity, bool& tma_pending, uint32_t* s_word, float* s_red, uint32_t* s_krange,
-                           uint32_t wave, uint32_t epoch, uint32_t wave_jobs) {
+                           uint32_t wave, uint32_t epoch) {
     using G = TileGeom<B>;
     int const tid = threadIdx.x;
     uint32_t const ii = inst_of(s, tile);
@@ -410,15 +410,8 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         }
     }
     if (s.learn.params && !s.learn.veto) {  // score policy: score what this solve queued, a warp per tile
-        // A solve that ends after half the CTAs with jobs this wave have
-        // reached the wave barrier (CTAs without one arrive at once) is
-        // likely one the wave waits for: its queued tiles keep no score and
-        // go by key, so scoring does not lengthen the wave.
-        if (tid == 0) s_word[2] = ld_relaxed(&s.ctl->bar_count);
         __syncthreads();
-        uint32_t const busy = min(wave_jobs, gridDim.x);
-        bool const late = 2u * (s_word[2] - min(s_word[2], gridDim.x - busy)) > busy;
-        for (int q = tid >> 5; q < 4 && !late; q += G::THREADS / 32)
+        for (int q = tid >> 5; q < 4; q += G::THREADS / 32)
             if (sm.queued[q] != kNone)
                 score_queued_warp(s, I, sm.queued[q], tc.tx + (q == 2) - (q == 0), tc.ty + (q == 3) - (q == 1), nxt,
                                   sm.queued_pos[q], wave + 1u);

@@ -317,16 +317,14 @@ def test_update_bounds_keep_parity(setups, medium, refresh, block, kernel):
 @pytest.mark.parametrize("kernel", [g.Kernel.Systolic, g.Kernel.FIM])
 @pytest.mark.parametrize("block", [8, 16])
 def test_sweep_caps_terminate_with_parity(setups, medium, mult, kernel, block):
-    """Inner-sweep caps at which most block-solves finish (the tile side and
-    twice it for 16 x 16 tiles; twice and four times it for 8 x 8 tiles, whose
-    one-warp solver moves information a cell per sweep) re-queue the capped
-    tiles; the solve still ends, within a wave bound that turns a
+    """Inner-sweep caps at which most block-solves finish (twice and four
+    times the tile side) re-queue the capped tiles; the solve still ends, within a wave bound that turns a
     non-terminating schedule into GHCM_ERR_NOT_CONVERGED instead of a hang,
     and keeps parity. Tighter caps leave most solves capped, each ending on a
     lower-only sweep, and drift further from the FIM (8 sweeps on 8 x 8 tiles
-    measured 1.56e-5 on the 1024^2 rings); test_small_sweep_caps_terminate
-    covers them."""
-    cap = mult * block * (2 if block == 8 else 1)
+    measured 1.56e-5, 16 on 16 x 16 tiles 1.04e-5, on the 1024^2 rings);
+    test_small_sweep_caps_terminate covers them."""
+    cap = mult * 2 * block
     for case in ("ring7_1024", "noise_1024"):
         speed, cost, seeds, ref = medium[case]
         s = setups(block, kernel, max_jobs=1024, max_sweeps=cap, max_waves=200000)
