@@ -639,8 +639,12 @@ def run_maze(args, world, rank, local) -> int:
     d_time = torch.empty_like(d_speed)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     t0 = time.perf_counter()
-    tuned, trials = g.autotune_batch(g.HcmConfig(block_size=16, fim_minimum_change=EPS),
-                                     [g.DeviceInstance(d_speed, d_seeds, d_time)], reps=1)
+    if args.no_autotune:  # a fixed config (e.g. for a profiler capture of the timed launches)
+        tuned, trials = g.HcmConfig(block_size=args.block, max_jobs=args.n, max_sweeps=args.sweeps,
+                                    fim_minimum_change=EPS), []
+    else:
+        tuned, trials = g.autotune_batch(g.HcmConfig(block_size=16, fim_minimum_change=EPS),
+                                         [g.DeviceInstance(d_speed, d_seeds, d_time)], reps=1)
     tune_s = time.perf_counter() - t0
     block, n = tuned.block_size, tuned.max_jobs
     plain_cfg = g.HcmConfig(block_size=block, max_jobs=n, max_sweeps=tuned.max_sweeps, kernel=tuned.kernel,
@@ -1122,7 +1126,8 @@ def main() -> int:
                     help="default workload: the headline pair only (no other n, veto policy or ring sub-objects)")
     ap.add_argument("--workload", default="noise", choices=["noise", "ring", "batched", "maze"])
     ap.add_argument("--no-autotune", action="store_true",
-                    help="batched workload: use --block and --n instead of the autotuner's choice")
+                    help="batched and maze workloads: use --block, --n (and --sweeps) instead of the autotuner's choice")
+    ap.add_argument("--sweeps", type=int, default=0, help="maze workload with --no-autotune: the inner-sweep cap")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
