@@ -366,8 +366,8 @@ def reference_schedule(o, cost, seeds, block: int, n: int, wg: int, fim) -> dict
             "note": "CPU restatement; the wave's jobs run one after another"}
 
 
-def _learned_setup(g, learned, params, threshold, policy, **kw):
-    cfg = g.HcmConfig(block_size=BLOCK, fim_minimum_change=EPS, schedule=g.Schedule.Learned, **kw)
+def _learned_setup(g, learned, params, threshold, policy, block: int = BLOCK, **kw):
+    cfg = g.HcmConfig(block_size=block, fim_minimum_change=EPS, schedule=g.Schedule.Learned, **kw)
     s = g.HcmSetup(cfg)
     learned.set_model(s, params, threshold)
     learned.set_policy(s, policy)
@@ -657,7 +657,7 @@ def run_maze(args, world, rank, local) -> int:
         # the tuned n caps the wave and waves with fewer qualifying tiles are
         # filled to n in key order (the best of a cap / fill / threshold sweep
         # on this field: 141 waves against the plain schedule's 172)
-        s_learned = _learned_setup(g, learned, params, threshold, learned.POLICY_SCORE, max_jobs=n,
+        s_learned = _learned_setup(g, learned, params, threshold, learned.POLICY_SCORE, block=block, max_jobs=n,
                                    fallback_jobs=n, max_sweeps=tuned.max_sweeps)
     head = s_learned if s_learned is not None else s_plain
     d_time_p = torch.empty_like(d_speed)
