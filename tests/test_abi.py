@@ -180,3 +180,21 @@ def test_noalloc_rejects_sizes_that_wrap_before_any_launch(ghcm_lib):
     for w, h in ((0xFFFFFFFF, 1), (1, 0xFFFFFFFF), (0xFFFFFFF1, 0xFFFFFFF1), (1 << 31, 2)):
         rc = ghcm_lib.ghcm_solve_device_noalloc(ctypes.byref(c), dummy, 1, w, h, 1.0, dummy, 1, dummy, None)
         assert rc == _lib.GHCM_ERR_TOO_LARGE, (w, h, rc)
+
+
+def test_refresh_modes_pass_the_config_check(ghcm_lib):
+    """The named update-bound modes and 1..15 pass the config check (without a
+    GPU ghcm_create then stops at the device, never at the config); 16 and
+    other values are bad arguments."""
+    c = _lib.GhcmConfig()
+    ghcm_lib.ghcm_config_default(ctypes.byref(c))
+    h = ctypes.c_void_p()
+    for ok in (0, 1, 15, _lib.GHCM_REFRESH_OFF, _lib.GHCM_REFRESH_IN_SOLVE):
+        c.refresh_solves = ok
+        rc = ghcm_lib.ghcm_create(ctypes.byref(c), ctypes.byref(h))
+        assert rc != _lib.GHCM_ERR_BAD_ARG, ok
+        if rc == 0:
+            ghcm_lib.ghcm_destroy(h)
+    for bad in (16, 1000, 0xFFFFFFFD):
+        c.refresh_solves = bad
+        assert ghcm_lib.ghcm_create(ctypes.byref(c), ctypes.byref(h)) == _lib.GHCM_ERR_BAD_ARG, bad

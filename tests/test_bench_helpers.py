@@ -66,3 +66,13 @@ def test_headline_traffic_comes_from_the_committed_capture():
     t = bench.load_traffic("k_solve_noise4096_learned.json")
     assert t == pytest.approx(d["dram_bytes_read"] + d["dram_bytes_write"]) and t > 0
     assert d["block_solves"] > 0
+
+
+def test_maze_traffic_scales_by_block_solves():
+    d = json.loads((PROFILES / "k_solve_maze16384.json").read_text())
+    assert bench.load_traffic("k_solve_maze16384.json", block=32, n=9728) == pytest.approx(d["dram_bytes_per_launch"])
+    assert bench.load_traffic("k_solve_maze16384.json", block=16) is None
+    assert bench.load_block_solves("k_solve_maze16384.json") == d["block_solves"] > 0
+    assert bench.load_block_solves("no_such_capture.json") is None
+    # bytes per block-solve at least the algorithmic 12,800 B of a 32 x 32 tile
+    assert d["dram_bytes_per_launch"] / d["block_solves"] >= bench.bytes_per_solve(32)
