@@ -138,7 +138,7 @@ struct ScoreGate {
 // jobs are m - carried.
 constexpr int SELECT_BINS = 2048;
 
-template <int THREADS, int CACHE>
+template <int THREADS, int CACHE, int UNROLL>
 __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_t n, uint32_t* s_hist, uint32_t* s_sel,
                                  float lo, float hi, bool have_range, uint32_t jobs_base, ScoreGate gate) {
     __shared__ float s_fmin[THREADS / 32], s_fmax[THREADS / 32];
@@ -211,18 +211,24 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
         for (int u = 0; u < CACHE; ++u)
             if (tid + u * THREADS < m) atomicAdd(&s_hist[cb[u]], 1u);
     } else {
-        uint32_t i = tid;
-        for (; i + 3u * THREADS < m; i += 4u * THREADS) {
-            uint32_t t4[4];
+        // UNROLL entries in flight per thread: ids, then keys, each one round trip
+        for (uint32_t i0 = 0; i0 < m; i0 += UNROLL * THREADS) {
+            uint32_t tu[UNROLL];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) t4[u] = __ldcg(&list[i + u * THREADS]);
-            int b4[4];
+            for (int u = 0; u < UNROLL; ++u) {
+                uint32_t const i = i0 + tid + u * THREADS;
+                tu[u] = (i < m) ? __ldcg(&list[i]) : 0u;
+            }
+            int bu[UNROLL];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) b4[u] = bin_of(i + u * THREADS, t4[u]);
+            for (int u = 0; u < UNROLL; ++u) {
+                uint32_t const i = i0 + tid + u * THREADS;
+                bu[u] = (i < m) ? bin_of(i, tu[u]) : -1;
+            }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) atomicAdd(&s_hist[b4[u]], 1u);
+            for (int u = 0; u < UNROLL; ++u)
+                if (bu[u] >= 0) atomicAdd(&s_hist[bu[u]], 1u);
         }
-        for (; i < m; i += THREADS) atomicAdd(&s_hist[bin_of(i, __ldcg(&list[i]))], 1u);
     }
     __syncthreads();
     if (gate.on) n = max(min(s_hist[0], gate.cap), n);  // qualifying tiles first, up to the cap
@@ -290,20 +296,22 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
             if (i < m) place(i, __ldcg(&list[i]), cb[u]);
         }
     } else {
-        uint32_t i = tid;
-        for (; i + 3u * THREADS < m; i += 4u * THREADS) {  // four entries in flight per thread
-            uint32_t t4[4];
+        for (uint32_t i0 = 0; i0 < m; i0 += UNROLL * THREADS) {  // UNROLL entries in flight per thread
+            uint32_t tu[UNROLL];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) t4[u] = __ldcg(&list[i + u * THREADS]);
-            int b4[4];
+            for (int u = 0; u < UNROLL; ++u) {
+                uint32_t const i = i0 + tid + u * THREADS;
+                tu[u] = (i < m) ? __ldcg(&list[i]) : 0u;
+            }
+            int bu[UNROLL];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) b4[u] = bin_of(i + u * THREADS, t4[u]);
+            for (int u = 0; u < UNROLL; ++u) {
+                uint32_t const i = i0 + tid + u * THREADS;
+                bu[u] = (i < m) ? bin_of(i, tu[u]) : -1;
+            }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) place(i + u * THREADS, t4[u], b4[u]);
-        }
-        for (; i < m; i += THREADS) {
-            uint32_t const t = __ldcg(&list[i]);
-            place(i, t, bin_of(i, t));
+            for (int u = 0; u < UNROLL; ++u)
+                if (bu[u] >= 0) place(i0 + tid + u * THREADS, tu[u], bu[u]);
         }
     }
     if (gate.on && tid == 0) s_sel[5] = s_hist[0];  // qualifying tiles, for the counters
@@ -358,7 +366,7 @@ __device__ __forceinline__ float ld_relaxed_f(const float* p) { return __uint_as
 // JOBS phase (or, with no jobs before them and m <= n, the list itself), the
 // rest is carried to list[L ^ 1], where the activations of that phase also
 // go. Returns {in_list, job count} in s_sel[8], [11].
-template <int THREADS, int CACHE>
+template <int THREADS, int CACHE, int UNROLL>
 __device__ void plan_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t n, uint32_t base, float lo, float hi,
                           uint32_t* s_hist, uint32_t* s_sel, ScoreGate gate) {
     Ctl* ctl = s.ctl;
@@ -366,7 +374,7 @@ __device__ void plan_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t n, ui
     uint32_t carried = 0u;
     uint32_t qualifying = 0u;  // learned schedule: tiles scoring at or above the threshold
     if (!all) {
-        carried = select_top_n<THREADS, CACHE>(s, L, m, n, s_hist, s_sel, lo, hi, s.key_mode == 0u, base, gate);
+        carried = select_top_n<THREADS, CACHE, UNROLL>(s, L, m, n, s_hist, s_sel, lo, hi, s.key_mode == 0u, base, gate);
         if (gate.on) qualifying = s_sel[5];
     } else {
         if (base)
@@ -401,7 +409,7 @@ __device__ void plan_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t n, ui
 //     empty after RESIDUAL    -> DONE
 // The key range of list[act] comes from the activations (ctl->krange); its
 // min and span are published as this wave's front for the features.
-template <int THREADS, int CACHE>
+template <int THREADS, int CACHE, int UNROLL>
 __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_hist, uint32_t* s_sel) {
     Ctl* ctl = s.ctl;
     int const tid = threadIdx.x;
@@ -461,7 +469,7 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
             ScoreGate gate{scored, 0.f, s.max_jobs};
             if (scored) gate.thr = logf(s.learn.threshold / (1.f - s.learn.threshold));
             uint32_t const n = scored ? min(s.learn.fallback_jobs, s.max_jobs) : s.max_jobs;
-            plan_jobs<THREADS, CACHE>(s, act, m, n, 0u, lo, hi, s_hist, s_sel, gate);
+            plan_jobs<THREADS, CACHE, UNROLL>(s, act, m, n, 0u, lo, hi, s_hist, s_sel, gate);
             if (tid == 0) atomicAdd(&ctl->waves, 1u);
 #ifdef GHCM_PROFILE
             if (tid == 0) {  // [20] decision loads, [21] job planning, [22] waves that ran the top-n select
@@ -524,7 +532,7 @@ __device__ uint32_t sm_rank(const Ctl* ctl, const uint32_t* s_slot, uint32_t* s_
 // that carries the decision, so a released CTA needs no further load. The
 // waits are bounded. On return s_state holds the new state; returns false
 // when the grid must stop (timeout or error).
-template <int THREADS, int CACHE>
+template <int THREADS, int CACHE, int UNROLL>
 __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, uint32_t* s_state,
                              uint32_t* s_krange) {
     __shared__ uint32_t s_last;
@@ -560,7 +568,7 @@ __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, 
             ctl->prof[14] = ctl->prof[16] = ctl->prof[18] = 0ull;
         }
 #endif
-        decide_phase<THREADS, CACHE>(s, s_state, s_hist, s_sel);
+        decide_phase<THREADS, CACHE, UNROLL>(s, s_state, s_hist, s_sel);
         __syncthreads();
         if (threadIdx.x == 0) {
             // errors raised before the arrivals, or the wave cap just hit

@@ -108,7 +108,9 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, CTAS) k_solve(const __gr
     bool ranked = false;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
-        bool const ok = wave_barrier<G::THREADS, select_cache<B, FIM>()>(s, s_hist, s_sel, s_state, s_krange);
+        // uncached select entries in flight per thread: fewer in the 32-register builds
+        bool const ok =
+            wave_barrier<G::THREADS, select_cache<B, FIM>(), (CTAS > 4 ? 4 : 8)>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
         if (!ranked) {  // the first barrier follows every CTA's sm_enter
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
     bool ranked = false;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
-        bool const ok = wave_barrier<W::THREADS, 4>(s, s_hist, s_sel, s_state, s_krange);
+        bool const ok = wave_barrier<W::THREADS, 4, 8>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
         if (!ranked) {
