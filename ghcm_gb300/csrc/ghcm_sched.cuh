@@ -131,14 +131,28 @@ struct ScoreGate {
 // a histogram of SELECT_BINS bins over [lo, hi] (the keys' range, or a
 // superset of it; with have_range false a first pass finds it), a scan for
 // the bin holding the n-th key, then every tile of a lower bin and enough
-// tiles of that bin (in list order) go to s.jobs from jobs_base, the rest to
-// list[L ^ 1]. The order is exact up to 1/SELECT_BINS of the range. With the
+// tiles of that bin go to s.jobs from jobs_base, the rest to list[L ^ 1].
+// The order is exact up to 1/SELECT_BINS of the range. With the
 // gate on, bin 0 holds the qualifying tiles and the keys use the others; n
 // becomes max(min(qualifying, cap), n). Returns the number carried; the
 // jobs are m - carried.
 constexpr int SELECT_BINS = 2048;
 
-template <int THREADS, int CACHE, int UNROLL>
+// Position of this lane's item among a warp's items, counted from *ctr: one
+// shared-memory atomic per warp instead of one per item. Every lane of the
+// warp calls it; lanes with want false get an unspecified value.
+__device__ __forceinline__ uint32_t warp_slot(uint32_t* ctr, bool want) {
+    uint32_t const mask = __ballot_sync(0xffffffffu, want);
+    if (mask == 0u) return 0u;
+    int const lane = threadIdx.x & 31;
+    int const leader = __ffs(mask) - 1;
+    uint32_t base = 0u;
+    if (lane == leader) base = atomicAdd(ctr, static_cast<uint32_t>(__popc(mask)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + static_cast<uint32_t>(__popc(mask & ((1u << lane) - 1u)));
+}
+
+template <int THREADS, int R>
 __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_t n, uint32_t* s_hist, uint32_t* s_sel,
                                  float lo, float hi, bool have_range, uint32_t jobs_base, ScoreGate gate) {
     __shared__ float s_fmin[THREADS / 32], s_fmax[THREADS / 32];
@@ -182,52 +196,49 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
     int const first = gate.on ? 1 : 0;  // bins of the keys: [first, SELECT_BINS)
     float const span = hi - lo;
     float const scale = (span > 0.f) ? static_cast<float>(SELECT_BINS - 1 - first) / span : 0.f;
-    auto bin_of = [&](uint32_t i, uint32_t t) -> int {
-        if (gate.on && __ldcg(&score[i]) >= gate.thr) return 0;  // +inf for tiles re-queued in full
-        float const k = __uint_as_float(tile_key(s, t));
-        if (!(k < f_inf())) return SELECT_BINS - 1;
-        int const b = first + static_cast<int>((k - lo) * scale);
-        return b < first ? first : (b >= SELECT_BINS ? SELECT_BINS - 1 : b);
+    // Entries i0 + tid + u * THREADS (u < R): ids and, with the gate on,
+    // scores in one round trip, then the keys in a second; b = -1 past m.
+    auto load = [&](uint32_t i0, uint32_t (&t)[R], int (&b)[R]) {
+        bool q[R];
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            uint32_t const i = i0 + tid + u * THREADS;
+            t[u] = (i < m) ? __ldcg(&list[i]) : 0u;
+            q[u] = gate.on && i < m && __ldcg(&score[i]) >= gate.thr;  // +inf: re-queued in full
+        }
+        uint32_t kb[R];
+#pragma unroll
+        for (int u = 0; u < R; ++u) kb[u] = (i0 + tid + u * THREADS < m) ? tile_key(s, t[u]) : inf_bits();
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            float const k = __uint_as_float(kb[u]);
+            int bb = SELECT_BINS - 1;
+            if (q[u]) {
+                bb = 0;
+            } else if (k < f_inf()) {
+                bb = first + static_cast<int>((k - lo) * scale);
+                bb = bb < first ? first : (bb >= SELECT_BINS ? SELECT_BINS - 1 : bb);
+            }
+            b[u] = (i0 + tid + u * THREADS < m) ? bb : -1;
+        }
     };
-    // pass 2: histogram. Up to CACHE entries per thread (a register budget set
-    // by the kernel) keep their bin in registers for the gather pass (lists
-    // of up to THREADS * CACHE tiles), so it re-reads only the coalesced list;
-    // longer lists find bins again there.
-    bool const cached = m <= static_cast<uint32_t>(THREADS * CACHE);
-    int cb[CACHE];
-    if (cached) {
-        uint32_t ct[CACHE];
+    // pass 2: histogram. The first R * THREADS entries keep their ids and
+    // bins in registers for the gather; longer lists find them again there.
+    bool const held = m <= static_cast<uint32_t>(R * THREADS);
+    uint32_t t[R];
+    int b[R];
+    load(0u, t, b);
 #pragma unroll
-        for (int u = 0; u < CACHE; ++u) {
-            uint32_t const i = tid + u * THREADS;
-            ct[u] = (i < m) ? __ldcg(&list[i]) : 0u;
-        }
+    for (int u = 0; u < R; ++u)
+        if (b[u] >= 0) atomicAdd(&s_hist[b[u]], 1u);
+    if (!held) {
+        for (uint32_t i0 = R * THREADS; i0 < m; i0 += R * THREADS) {
+            uint32_t t2[R];
+            int b2[R];
+            load(i0, t2, b2);
 #pragma unroll
-        for (int u = 0; u < CACHE; ++u) {
-            uint32_t const i = tid + u * THREADS;
-            cb[u] = (i < m) ? bin_of(i, ct[u]) : 0;
-        }
-#pragma unroll
-        for (int u = 0; u < CACHE; ++u)
-            if (tid + u * THREADS < m) atomicAdd(&s_hist[cb[u]], 1u);
-    } else {
-        // UNROLL entries in flight per thread: ids, then keys, each one round trip
-        for (uint32_t i0 = 0; i0 < m; i0 += UNROLL * THREADS) {
-            uint32_t tu[UNROLL];
-#pragma unroll
-            for (int u = 0; u < UNROLL; ++u) {
-                uint32_t const i = i0 + tid + u * THREADS;
-                tu[u] = (i < m) ? __ldcg(&list[i]) : 0u;
-            }
-            int bu[UNROLL];
-#pragma unroll
-            for (int u = 0; u < UNROLL; ++u) {
-                uint32_t const i = i0 + tid + u * THREADS;
-                bu[u] = (i < m) ? bin_of(i, tu[u]) : -1;
-            }
-#pragma unroll
-            for (int u = 0; u < UNROLL; ++u)
-                if (bu[u] >= 0) atomicAdd(&s_hist[bu[u]], 1u);
+            for (int u = 0; u < R; ++u)
+                if (b2[u] >= 0) atomicAdd(&s_hist[b2[u]], 1u);
         }
     }
     __syncthreads();
@@ -274,44 +285,35 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
     }
     int const bnd = static_cast<int>(s_sel[0]);
     uint32_t const take_eq = s_sel[1];
-    // pass 3: gather; a carried entry keeps its learned score
-    auto place = [&](uint32_t i, uint32_t t, int b) {
-        bool take = b < bnd;
-        if (!take && b == bnd) take = atomicAdd(&s_sel[2], 1u) < take_eq;
+    // pass 3: gather, positions by warp (every lane of a warp calls place for
+    // the same u). A carried entry keeps whether it qualified (+inf / -inf):
+    // the gate only compares scores with its fixed threshold.
+    auto place = [&](uint32_t tt, int bb) {
+        bool const valid = bb >= 0;
+        bool const eq = valid && bb == bnd;
+        uint32_t const e = warp_slot(&s_sel[2], eq);
+        bool const take = valid && (bb < bnd || (eq && e < take_eq));
+        uint32_t const pj = warp_slot(&s_sel[3], take);
+        uint32_t const pc = warp_slot(&s_sel[4], valid && !take);
         if (take) {
-            uint32_t const pos = jobs_base + atomicAdd(&s_sel[3], 1u);
-            if (GHCM_CHECK(s.ctl, pos < s.max_jobs, 9u)) s.jobs[pos] = t;
-        } else {
-            uint32_t const pos = atomicAdd(&s_sel[4], 1u);
-            if (GHCM_CHECK(s.ctl, pos < s.num_tiles, 10u)) {
-                carry[pos] = t;
-                if (score) carry_score[pos] = __ldcg(&score[i]);
+            uint32_t const pos = jobs_base + pj;
+            if (GHCM_CHECK(s.ctl, pos < s.max_jobs, 9u)) s.jobs[pos] = tt;
+        } else if (valid) {
+            if (GHCM_CHECK(s.ctl, pc < s.num_tiles, 10u)) {
+                carry[pc] = tt;
+                if (gate.on) carry_score[pc] = (bb == 0) ? f_inf() : -f_inf();
             }
         }
     };
-    if (cached) {
 #pragma unroll
-        for (int u = 0; u < CACHE; ++u) {
-            uint32_t const i = tid + u * THREADS;
-            if (i < m) place(i, __ldcg(&list[i]), cb[u]);
-        }
-    } else {
-        for (uint32_t i0 = 0; i0 < m; i0 += UNROLL * THREADS) {  // UNROLL entries in flight per thread
-            uint32_t tu[UNROLL];
+    for (int u = 0; u < R; ++u) place(t[u], b[u]);
+    if (!held) {
+        for (uint32_t i0 = R * THREADS; i0 < m; i0 += R * THREADS) {
+            uint32_t t2[R];
+            int b2[R];
+            load(i0, t2, b2);
 #pragma unroll
-            for (int u = 0; u < UNROLL; ++u) {
-                uint32_t const i = i0 + tid + u * THREADS;
-                tu[u] = (i < m) ? __ldcg(&list[i]) : 0u;
-            }
-            int bu[UNROLL];
-#pragma unroll
-            for (int u = 0; u < UNROLL; ++u) {
-                uint32_t const i = i0 + tid + u * THREADS;
-                bu[u] = (i < m) ? bin_of(i, tu[u]) : -1;
-            }
-#pragma unroll
-            for (int u = 0; u < UNROLL; ++u)
-                if (bu[u] >= 0) place(i0 + tid + u * THREADS, tu[u], bu[u]);
+            for (int u = 0; u < R; ++u) place(t2[u], b2[u]);
         }
     }
     if (gate.on && tid == 0) s_sel[5] = s_hist[0];  // qualifying tiles, for the counters
@@ -366,7 +368,7 @@ __device__ __forceinline__ float ld_relaxed_f(const float* p) { return __uint_as
 // JOBS phase (or, with no jobs before them and m <= n, the list itself), the
 // rest is carried to list[L ^ 1], where the activations of that phase also
 // go. Returns {in_list, job count} in s_sel[8], [11].
-template <int THREADS, int CACHE, int UNROLL>
+template <int THREADS, int R>
 __device__ void plan_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t n, uint32_t base, float lo, float hi,
                           uint32_t* s_hist, uint32_t* s_sel, ScoreGate gate) {
     Ctl* ctl = s.ctl;
@@ -374,7 +376,7 @@ __device__ void plan_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t n, ui
     uint32_t carried = 0u;
     uint32_t qualifying = 0u;  // learned schedule: tiles scoring at or above the threshold
     if (!all) {
-        carried = select_top_n<THREADS, CACHE, UNROLL>(s, L, m, n, s_hist, s_sel, lo, hi, s.key_mode == 0u, base, gate);
+        carried = select_top_n<THREADS, R>(s, L, m, n, s_hist, s_sel, lo, hi, s.key_mode == 0u, base, gate);
         if (gate.on) qualifying = s_sel[5];
     } else {
         if (base)
@@ -409,7 +411,7 @@ __device__ void plan_jobs(const Sched& s, uint32_t L, uint32_t m, uint32_t n, ui
 //     empty after RESIDUAL    -> DONE
 // The key range of list[act] comes from the activations (ctl->krange); its
 // min and span are published as this wave's front for the features.
-template <int THREADS, int CACHE, int UNROLL>
+template <int THREADS, int R>
 __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_hist, uint32_t* s_sel) {
     Ctl* ctl = s.ctl;
     int const tid = threadIdx.x;
@@ -469,13 +471,13 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
             ScoreGate gate{scored, 0.f, s.max_jobs};
             if (scored) gate.thr = logf(s.learn.threshold / (1.f - s.learn.threshold));
             uint32_t const n = scored ? min(s.learn.fallback_jobs, s.max_jobs) : s.max_jobs;
-            plan_jobs<THREADS, CACHE, UNROLL>(s, act, m, n, 0u, lo, hi, s_hist, s_sel, gate);
+            plan_jobs<THREADS, R>(s, act, m, n, 0u, lo, hi, s_hist, s_sel, gate);
             if (tid == 0) atomicAdd(&ctl->waves, 1u);
 #ifdef GHCM_PROFILE
             if (tid == 0) {  // [20] decision loads, [21] job planning, [22] waves that ran the top-n select
                 ctl->prof[20] += p_sel0 - ctl->prof[23];
                 ctl->prof[21] += global_ns() - p_sel0;
-                if (m > s.max_jobs) ctl->prof[22] += 1u;
+                if (m > n) ctl->prof[22] += 1u;
             }
 #endif
         }
@@ -532,7 +534,7 @@ __device__ uint32_t sm_rank(const Ctl* ctl, const uint32_t* s_slot, uint32_t* s_
 // that carries the decision, so a released CTA needs no further load. The
 // waits are bounded. On return s_state holds the new state; returns false
 // when the grid must stop (timeout or error).
-template <int THREADS, int CACHE, int UNROLL>
+template <int THREADS, int R>
 __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, uint32_t* s_state,
                              uint32_t* s_krange) {
     __shared__ uint32_t s_last;
@@ -568,7 +570,7 @@ __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, 
             ctl->prof[14] = ctl->prof[16] = ctl->prof[18] = 0ull;
         }
 #endif
-        decide_phase<THREADS, CACHE, UNROLL>(s, s_state, s_hist, s_sel);
+        decide_phase<THREADS, R>(s, s_state, s_hist, s_sel);
         __syncthreads();
         if (threadIdx.x == 0) {
             // errors raised before the arrivals, or the wave cap just hit

@@ -62,11 +62,12 @@ constexpr int max_ctas_per_sm() {
 // ms, at n=1024: 16.2 -> 16.5 ms), so those keep the 4-CTA build.
 constexpr int kWideCtas = 8;
 
-// Keys per thread the top-n select keeps in registers between its passes: as
-// many as fit in the kernel's register budget without spills.
-template <int B, bool FIM>
-__host__ __device__ constexpr int select_cache() {
-    return B == 32 ? (FIM ? 1 : 2) : 4;
+// List entries per thread the top-n select keeps in registers between its
+// passes (ids and bins; a list of up to 256 x this many is read once): 7 in
+// the 64-register builds (8 spills), 4 in the 32-register wide builds.
+template <int CTAS>
+__host__ __device__ constexpr int select_regs() {
+    return CTAS > 4 ? 4 : 7;
 }
 
 template <int B, bool FIM, int CTAS = max_ctas_per_sm<B>()>
@@ -108,9 +109,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, CTAS) k_solve(const __gr
     bool ranked = false;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
-        // uncached select entries in flight per thread: fewer in the 32-register builds
-        bool const ok =
-            wave_barrier<G::THREADS, select_cache<B, FIM>(), (CTAS > 4 ? 4 : 8)>(s, s_hist, s_sel, s_state, s_krange);
+        bool const ok = wave_barrier<G::THREADS, select_regs<CTAS>()>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
         if (!ranked) {  // the first barrier follows every CTA's sm_enter
@@ -203,7 +202,7 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
     bool ranked = false;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
-        bool const ok = wave_barrier<W::THREADS, 4, 8>(s, s_hist, s_sel, s_state, s_krange);
+        bool const ok = wave_barrier<W::THREADS, 8>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
         if (!ranked) {
