@@ -123,6 +123,11 @@ inline void print_profile(const Ctl& c, int grid) {
         std::fprintf(stderr, "[ghcm-prof] per wave, decision: control loads %.2f us, job planning %.2f us; "
                      "%.0f%% of waves ran the top-n select\n",
                      c.prof[20] / 1e3 / c.prof[9], c.prof[21] / 1e3 / c.prof[9], 100.0 * c.prof[22] / c.prof[9]);
+    if (c.prof[22])
+        std::fprintf(stderr, "[ghcm-prof] per top-n select: histogram %.2f us, scan %.2f us, gather %.2f us; "
+                     "per wave, decision end to release %.2f us\n",
+                     c.prof[24] / 1e3 / c.prof[22], c.prof[25] / 1e3 / c.prof[22], c.prof[26] / 1e3 / c.prof[22],
+                     c.prof[27] / 1e3 / std::max(1ull, c.prof[9]));
     if (c.prof[13])
         std::fprintf(stderr, "[ghcm-prof] per CTA block-solve: stage %.2f us, sweeps %.2f us (%.3f us/sweep), "
                      "probe+commit+activate %.2f us\n",

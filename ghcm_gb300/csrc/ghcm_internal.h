@@ -67,7 +67,7 @@ struct Ctl {
     uint32_t residual_passes;
     uint32_t max_active;
     unsigned long long block_solves;
-    unsigned long long prof[24];   // GHCM_PROFILE builds: per-phase nanoseconds and sweep counts
+    unsigned long long prof[32];   // GHCM_PROFILE builds: per-phase nanoseconds and sweep counts
     unsigned long long release_ns; // GHCM_PROFILE builds: when the last barrier was released
     uint32_t wave_max_sweeps;      // GHCM_PROFILE builds: most sweeps of one block-solve in this wave
     uint32_t check_site;           // GHCM_CHECKED builds: largest id of a failed index check

@@ -138,20 +138,6 @@ struct ScoreGate {
 // jobs are m - carried.
 constexpr int SELECT_BINS = 2048;
 
-// Position of this lane's item among a warp's items, counted from *ctr: one
-// shared-memory atomic per warp instead of one per item. Every lane of the
-// warp calls it; lanes with want false get an unspecified value.
-__device__ __forceinline__ uint32_t warp_slot(uint32_t* ctr, bool want) {
-    uint32_t const mask = __ballot_sync(0xffffffffu, want);
-    if (mask == 0u) return 0u;
-    int const lane = threadIdx.x & 31;
-    int const leader = __ffs(mask) - 1;
-    uint32_t base = 0u;
-    if (lane == leader) base = atomicAdd(ctr, static_cast<uint32_t>(__popc(mask)));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    return base + static_cast<uint32_t>(__popc(mask & ((1u << lane) - 1u)));
-}
-
 template <int THREADS, int R>
 __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_t n, uint32_t* s_hist, uint32_t* s_sel,
                                  float lo, float hi, bool have_range, uint32_t jobs_base, ScoreGate gate) {
@@ -162,6 +148,9 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
     uint32_t* carry = s.list[L ^ 1u];
     const float* score = s.learn.lscore[L];
     float* carry_score = s.learn.lscore[L ^ 1u];
+#ifdef GHCM_PROFILE
+    uint64_t const p_s0 = global_ns();
+#endif
     for (int i = tid; i < SELECT_BINS; i += THREADS) s_hist[i] = 0u;
     if (!have_range) {
         // pass 1: range of the finite keys
@@ -241,8 +230,6 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
                 if (b2[u] >= 0) atomicAdd(&s_hist[b2[u]], 1u);
         }
     }
-    __syncthreads();
-    if (gate.on) n = max(min(s_hist[0], gate.cap), n);  // qualifying tiles first, up to the cap
     if (tid == 0) {
         s_sel[0] = SELECT_BINS;  // n >= m: every bin lies below the boundary
         s_sel[1] = 0u;
@@ -251,12 +238,19 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
         s_sel[4] = 0u;
     }
     __syncthreads();
+#ifdef GHCM_PROFILE
+    uint64_t const p_s1 = global_ns();
+#endif
+    if (gate.on) n = max(min(s_hist[0], gate.cap), n);  // qualifying tiles first, up to the cap
     if (n < m) {
         // the bin holding the n-th smallest entry: thread t scans bins [t*PER, (t+1)*PER)
         constexpr int PER = SELECT_BINS / THREADS;
+        uint32_t hv[PER];  // scalar reads: s_hist is only 4-byte aligned
+#pragma unroll
+        for (int j = 0; j < PER; ++j) hv[j] = s_hist[tid * PER + j];
         uint32_t part = 0u;
 #pragma unroll
-        for (int j = 0; j < PER; ++j) part += s_hist[tid * PER + j];
+        for (int j = 0; j < PER; ++j) part += hv[j];
         uint32_t incl = part;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -272,7 +266,7 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
         if (below < n && n <= below + part) {
 #pragma unroll
             for (int j = 0; j < PER; ++j) {
-                uint32_t const h = s_hist[tid * PER + j];
+                uint32_t const h = hv[j];
                 if (below + h >= n) {
                     s_sel[0] = static_cast<uint32_t>(tid * PER + j);
                     s_sel[1] = n - below;  // how many of the boundary bin to take
@@ -285,39 +279,72 @@ __device__ uint32_t select_top_n(const Sched& s, uint32_t L, uint32_t m, uint32_
     }
     int const bnd = static_cast<int>(s_sel[0]);
     uint32_t const take_eq = s_sel[1];
-    // pass 3: gather, positions by warp (every lane of a warp calls place for
-    // the same u). A carried entry keeps whether it qualified (+inf / -inf):
-    // the gate only compares scores with its fixed threshold.
-    auto place = [&](uint32_t tt, int bb) {
-        bool const valid = bb >= 0;
-        bool const eq = valid && bb == bnd;
-        uint32_t const e = warp_slot(&s_sel[2], eq);
-        bool const take = valid && (bb < bnd || (eq && e < take_eq));
-        uint32_t const pj = warp_slot(&s_sel[3], take);
-        uint32_t const pc = warp_slot(&s_sel[4], valid && !take);
-        if (take) {
-            uint32_t const pos = jobs_base + pj;
-            if (GHCM_CHECK(s.ctl, pos < s.max_jobs, 9u)) s.jobs[pos] = tt;
-        } else if (valid) {
-            if (GHCM_CHECK(s.ctl, pc < s.num_tiles, 10u)) {
-                carry[pc] = tt;
-                if (gate.on) carry_score[pc] = (bb == 0) ? f_inf() : -f_inf();
+#ifdef GHCM_PROFILE
+    uint64_t const p_s2 = global_ns();
+#endif
+    // pass 3: gather. An entry of the boundary bin takes its turn with its own
+    // shared atomic (the first take_eq go); a warp then takes its job and
+    // carry positions for all R entries of each lane with one atomic each. A
+    // carried entry keeps whether it qualified (+inf / -inf): the gate only
+    // compares scores with its fixed threshold.
+    auto gather = [&](const uint32_t (&tt)[R], const int (&bb)[R]) {
+        uint32_t const lt = (1u << lane) - 1u;
+        bool tk[R];
+        uint32_t ntake = 0u, ncarry = 0u;
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            bool const valid = bb[u] >= 0;
+            bool take = valid && bb[u] < bnd;
+            if (valid && bb[u] == bnd) take = atomicAdd(&s_sel[2], 1u) < take_eq;
+            tk[u] = take;
+            ntake += __popc(__ballot_sync(0xffffffffu, take));
+            ncarry += __popc(__ballot_sync(0xffffffffu, valid && !take));
+        }
+        uint32_t jb = 0u, cb = 0u;
+        if (lane == 0) {
+            if (ntake) jb = atomicAdd(&s_sel[3], ntake);
+            if (ncarry) cb = atomicAdd(&s_sel[4], ncarry);
+        }
+        jb = jobs_base + __shfl_sync(0xffffffffu, jb, 0);
+        cb = __shfl_sync(0xffffffffu, cb, 0);
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            bool const valid = bb[u] >= 0;
+            uint32_t const tm = __ballot_sync(0xffffffffu, tk[u]);
+            uint32_t const cm = __ballot_sync(0xffffffffu, valid && !tk[u]);
+            if (tk[u]) {
+                uint32_t const pos = jb + __popc(tm & lt);
+                if (GHCM_CHECK(s.ctl, pos < s.max_jobs, 9u)) s.jobs[pos] = tt[u];
+            } else if (valid) {
+                uint32_t const pos = cb + __popc(cm & lt);
+                if (GHCM_CHECK(s.ctl, pos < s.num_tiles, 10u)) {
+                    carry[pos] = tt[u];
+                    if (gate.on) carry_score[pos] = (bb[u] == 0) ? f_inf() : -f_inf();
+                }
             }
+            jb += __popc(tm);
+            cb += __popc(cm);
         }
     };
-#pragma unroll
-    for (int u = 0; u < R; ++u) place(t[u], b[u]);
+    gather(t, b);
     if (!held) {
         for (uint32_t i0 = R * THREADS; i0 < m; i0 += R * THREADS) {
             uint32_t t2[R];
             int b2[R];
             load(i0, t2, b2);
-#pragma unroll
-            for (int u = 0; u < R; ++u) place(t2[u], b2[u]);
+            gather(t2, b2);
         }
     }
     if (gate.on && tid == 0) s_sel[5] = s_hist[0];  // qualifying tiles, for the counters
     __syncthreads();
+#ifdef GHCM_PROFILE
+    if (tid == 0) {  // [24] histogram, [25] scan, [26] gather
+        uint64_t const p_s3 = global_ns();
+        s.ctl->prof[24] += p_s1 - p_s0;
+        s.ctl->prof[25] += p_s2 - p_s1;
+        s.ctl->prof[26] += p_s3 - p_s2;
+    }
+#endif
     return s_sel[4];
 }
 
@@ -424,7 +451,9 @@ __device__ void decide_phase(const Sched& s, const uint32_t* st, uint32_t* s_his
         if (tid == 0) ctl->prof[23] = global_ns();  // decision start
 #endif
         // every control word the decision reads, in one round trip
-        uint32_t const m = ld_relaxed(&ctl->count[act]);
+        // a list holds each tile at most once; an overflow (an internal error,
+        // already flagged by activate) never makes the select read past it
+        uint32_t const m = min(ld_relaxed(&ctl->count[act]), s.num_tiles);
         uint32_t const klo = ld_relaxed(&ctl->krange[act][0]);
         uint32_t const khi = ld_relaxed(&ctl->krange[act][1]);
         if (tid == 0) s_sel[12] = ld_relaxed(&ctl->error);
@@ -571,6 +600,9 @@ __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, 
         }
 #endif
         decide_phase<THREADS, R>(s, s_state, s_hist, s_sel);
+#ifdef GHCM_PROFILE
+        uint64_t const t_dec = global_ns();
+#endif
         __syncthreads();
         if (threadIdx.x == 0) {
             // errors raised before the arrivals, or the wave cap just hit
@@ -580,6 +612,7 @@ __device__ bool wave_barrier(const Sched& s, uint32_t* s_hist, uint32_t* s_sel, 
 #ifdef GHCM_PROFILE
             uint64_t const t_rel = global_ns();
             ctl->prof[2] += t_rel - t_last;  // decide
+            ctl->prof[27] += t_rel - t_dec;  // end of the decision -> release store issued
             ctl->prof[9] += 1u;
             ctl->release_ns = t_rel;
 #endif

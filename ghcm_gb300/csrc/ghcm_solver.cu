@@ -64,10 +64,11 @@ constexpr int kWideCtas = 8;
 
 // List entries per thread the top-n select keeps in registers between its
 // passes (ids and bins; a list of up to 256 x this many is read once): 7 in
-// the 64-register builds (8 spills), 4 in the 32-register wide builds.
-template <int CTAS>
+// the 64-register systolic builds (8 spills), 6 in the block-FIM ones, 4 in
+// the 32-register wide builds.
+template <bool FIM, int CTAS>
 __host__ __device__ constexpr int select_regs() {
-    return CTAS > 4 ? 4 : 7;
+    return CTAS > 4 ? 4 : (FIM ? 6 : 7);
 }
 
 template <int B, bool FIM, int CTAS = max_ctas_per_sm<B>()>
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, CTAS) k_solve(const __gr
     bool ranked = false;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
-        bool const ok = wave_barrier<G::THREADS, select_regs<CTAS>()>(s, s_hist, s_sel, s_state, s_krange);
+        bool const ok = wave_barrier<G::THREADS, select_regs<FIM, CTAS>()>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
         if (!ranked) {  // the first barrier follows every CTA's sm_enter
@@ -135,7 +136,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, CTAS) k_solve(const __gr
                     if (tid == 0) atomicOr(&ctl->error, kErrInternal);
                     break;
                 }
-                int const r = solve_tile<B, FIM>(s, job, cur ^ 1u, sm, &s_bar, parity, tma_pending, s_word, s_red,
+                int const r = solve_tile<B, FIM, (CTAS <= 4)>(s, job, cur ^ 1u, sm, &s_bar, parity, tma_pending, s_word, s_red,
                                                  s_krange, wave, s_state[kStResid] + 1u);
                 if (r == kJobFailed) break;
                 solves += (r == kJobSolved) ? 1u : 0u;
@@ -323,13 +324,15 @@ __global__ void k_wait_selftest(const uint32_t* flag, Ctl* ctl, uint64_t timeout
 }
 
 // Every 32-bit pattern from `base` on (one per thread) through sqrt_rn and
-// through __fsqrt_rn; adds the number of inputs whose results differ (NaN
-// results compare equal) to *mismatches.
+// through __fsqrt_rn, and those in [2^-100, +inf) also through
+// sqrt_rn_normal; adds the number of inputs whose results differ (NaN results
+// compare equal) to *mismatches.
 __global__ void k_sqrt_selftest(uint32_t base, unsigned long long* mismatches) {
     uint32_t const i = base + blockIdx.x * blockDim.x + threadIdx.x;
     float const a = __uint_as_float(i);
     float const r = sqrt_rn(a), e = __fsqrt_rn(a);
-    bool const same = __float_as_uint(r) == __float_as_uint(e) || (isnan(r) && isnan(e));
+    bool same = __float_as_uint(r) == __float_as_uint(e) || (isnan(r) && isnan(e));
+    if (a >= 0x1p-100f && a < f_inf()) same &= __float_as_uint(sqrt_rn_normal(a)) == __float_as_uint(e);
     int const bad = __syncthreads_count(!same);
     if (threadIdx.x == 0 && bad) atomicAdd(mismatches, static_cast<unsigned long long>(bad));
 }

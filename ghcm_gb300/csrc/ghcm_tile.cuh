@@ -28,6 +28,8 @@
 // the second condition two converged tiles can keep activating each other.
 #pragma once
 
+#include <type_traits>
+
 #include "ghcm_learn.cuh"
 
 namespace ghcm {
@@ -72,7 +74,10 @@ enum : int { kJobFailed = 0, kJobSolved = 1, kJobDeferred = 2 };
 // kJobDeferred (the learned schedule's veto put it back in the active set) or
 // kJobFailed if the TMA stage timed out (the grid then stops at the next
 // barrier).
-template <int B, bool FIM>
+// NORMAL: the systolic sweep loop with the update's cases unfolded and a
+// short-root copy for tiles of normal costs; the 32-register wide builds,
+// where its extra registers spill, keep the plain loop.
+template <int B, bool FIM, bool NORMAL = true>
 __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<B>& sm, uint64_t* bar,
                            uint32_t& parity, bool& tma_pending, uint32_t* s_word, float* s_red, uint32_t* s_krange,
                            uint32_t wave, uint32_t epoch) {
@@ -211,7 +216,53 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     bool capped = false;
     uint32_t sweeps = 0;
 
-    if (!FIM) {
+    if (!FIM && NORMAL) {
+        // The sweep loop, with next_time and moves unfolded for the solve: b0
+        // is a cell's bound before the lower-only phase (+inf fresh, t0 in
+        // solve), keep says the phase has begun. A tile whose updatable costs
+        // are all normal_cost runs the update with the short square root.
+        float b0[G::CPT];
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < G::CPT; ++k) {
+            b0[k] = (mode == kUpdFresh) ? f_inf() : t0[k];
+            ok &= !v[k] || normal_cost(c[k]);
+        }
+        bool keep = mode == kUpdKeepMin;
+        auto sweep_loop = [&](auto normal) {
+            for (;;) {
+                bool moved = false;
+#pragma unroll
+                for (int k = 0; k < G::CPT; ++k) {
+                    if (!v[k]) continue;
+                    int const i = idx[k];
+                    float const ax = fminf(sm.time[i - 1], sm.time[i + 1]);
+                    float const ay = fminf(sm.time[i - BW], sm.time[i + BW]);
+                    float const raw = decltype(normal)::value ? godunov2_raw_normal(ax, ay, c[k], c2[k])
+                                                              : godunov2_raw(ax, ay, c[k], c2[k]);
+                    float const nt = fminf(keep ? t[k] : b0[k], raw);
+                    if (nt != t[k]) {
+                        float const d = __fsub_rn(nt, t[k]);  // nt != t: moves() without its equal case
+                        moved |= keep ? d < -eps : fabsf(d) > eps;
+                        t[k] = nt;
+                        sm.time[i] = nt;
+                        own_changed = true;
+                    }
+                }
+                ++sweeps;
+                if (!__syncthreads_or(moved)) break;
+                if (sweeps >= fresh_sweeps) keep = true;
+                if (sweeps >= s.max_sweeps) {
+                    capped = true;
+                    break;
+                }
+            }
+        };
+        if (__syncthreads_and(ok))
+            sweep_loop(std::true_type{});
+        else
+            sweep_loop(std::false_type{});
+    } else if (!FIM) {
         for (;;) {
             bool moved = false;
 #pragma unroll

@@ -346,10 +346,12 @@ int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_field, int 
 int ghcm_selftest_wait_timeout(ghcm_ctx* ctx, uint32_t timeout_ms);
 
 /* Self-test of the square root inside the device Godunov update: runs every
- * 32-bit float through it and through CUDA's IEEE __fsqrt_rn on ctx's device
- * and stores the number of inputs whose results differ (NaN results compare
- * equal) in *mismatches; 0 means the update's square root is the correctly
- * rounded one that the reference's update uses (src/eikonal.h:121-137).
+ * 32-bit float through it (both forms: the general one, and the short one
+ * used on [2^-100, +inf) for tiles of normal costs) and through CUDA's IEEE
+ * __fsqrt_rn on ctx's device and stores the number of inputs whose results
+ * differ (NaN results compare equal) in *mismatches; 0 means the update's
+ * square root is the correctly rounded one that the reference's update uses
+ * (src/eikonal.h:121-137).
  * Takes about 10 ms. */
 int ghcm_selftest_sqrt(ghcm_ctx* ctx, unsigned long long* mismatches);
 

@@ -136,6 +136,23 @@ def test_eps_zero_reaches_exact_fixed_point(setups, oracle_lib):
     check_field(res.field, oracle_lib.fim(cost, seeds, 0.0)[0], seeds)
 
 
+@pytest.mark.parametrize("block", [16, 32])
+def test_costs_outside_the_short_root_range(setups, oracle_lib, block):
+    """Tiles whose costs leave [2^-49, 2^63) (here 0, 1e-18 times the noise
+    costs and 1e19, where 2c^2 is still finite) sweep with the general square
+    root, the others with its short form: at eps = 0 every cell is an exact
+    fixed point of the reference update, and the field is within the bar of
+    the reference FIM."""
+    speed, seeds = fields.value_noise(300, seed=5, base_period=40.0, sources=4)
+    cost = fields.cost_from_speed(speed)
+    cost[0:64, 0:64] *= np.float32(1e-18)
+    cost[100:164, 100:164] = 0.0
+    cost[200:264, 16:80] = np.float32(1e19)
+    res = g.eikonal_hcm_cuda_ex(setups(block, fim_minimum_change=0.0), cost, seeds)
+    assert oracle_lib.residual(cost, res.field) == 0.0
+    check_field(res.field, oracle_lib.fim(cost, seeds, 0.0)[0], seeds)
+
+
 def test_workspace_reuse_across_sizes(setups, oracle_lib):
     s = setups(16)
     for n, w in ((300, 301), (40, 41), (520, 260), (17, 9)):
@@ -199,7 +216,9 @@ def test_bounded_wait_times_out_cleanly(setups):
 
 def test_update_sqrt_is_ieee_for_every_float(setups):
     """The device update's square root (an FMA-corrected hardware estimate)
-    gives the bits of CUDA's IEEE __fsqrt_rn for all 2^32 inputs."""
+    gives the bits of CUDA's IEEE __fsqrt_rn for all 2^32 inputs, and so does
+    its short form on [2^-100, +inf), which tiles of costs in [2^-49, 2^63)
+    use."""
     import ctypes
 
     s = setups(16)
