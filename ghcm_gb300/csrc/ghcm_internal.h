@@ -29,7 +29,10 @@ enum : uint32_t {
     kEdgeMask = 0xFu << 4,
     kSolveOne = 1u << 8,   // bits 8-11: the tile's block-solves so far, counted up to Sched::refresh
     kSolveMask = 0xFu << 8,
+    kActPhase0 = 1u << 12, // bits 12-15: a neighbour's solve activated the tile in a jobs phase whose
+    kActPhaseMask = 0xFu << 12,  // barrier generation is 0-3 mod 4 (kActPhase0 << gen % 4)
 };
+__host__ __device__ __forceinline__ uint32_t act_phase_bit(uint32_t gen) { return kActPhase0 << (gen & 3u); }
 constexpr uint32_t kMaxRefresh = 15;  // largest Sched::refresh the 4-bit solve count holds
 constexpr uint32_t kDefaultRefresh = 1;
 

@@ -223,7 +223,7 @@ __device__ __forceinline__ void learn_defer(const Sched& s, uint32_t tile, uint3
     __stcg(&s.learn.vetoes[tile], __ldcg(&s.learn.vetoes[tile]) + 1u);
     atomicMax(&s.learn.kmax[tile], kmax_bits);
     atomicAdd(&s.ctl->vetoes, 1u);
-    activate(s, tile, flags & (kFull | kEdgeMask), __uint_as_float(key_bits), nxt, s_krange);
+    activate(s, tile, flags & (kFull | kEdgeMask), __uint_as_float(key_bits), nxt, s_krange, 0u);
 }
 
 // Commit-time bookkeeping, by one thread: solve count, wave of the last

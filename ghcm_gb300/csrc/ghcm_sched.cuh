@@ -70,14 +70,16 @@ __device__ __forceinline__ float to_cost(const Inst& I, float v) {
 constexpr uint32_t kNoPos = 0xffffffffu;
 
 // Puts `tile` into the next active set: lowers its key to `key`, ORs `bits`
-// into its flags and appends it to list[nxt] unless it is already active.
+// (and `pbit`, act_phase_bit of the phase when a solve of this phase activates
+// a neighbour, else 0) into its flags and appends it to list[nxt] unless it
+// is already active.
 // The device form of the dirty-set test + heap push + border-mask OR of
 // src/eikonal_hcm.cpp:451-462. s_krange (the calling CTA's {min, max} key
 // bits of what it activated this phase) is widened to `key`. Returns the
 // tile's position in list[nxt] when this call appended it (it was idle),
 // else kNoPos.
 __device__ __forceinline__ uint32_t activate(const Sched& s, uint32_t tile, uint32_t bits, float key, uint32_t nxt,
-                                             uint32_t* s_krange) {
+                                             uint32_t* s_krange, uint32_t pbit) {
     uint32_t const kb = __float_as_uint(key);
     atomicMin(&s.key[tile], kb);
     if (s.learn.kmax) atomicMax(&s.learn.kmax[tile], kb);
@@ -85,7 +87,7 @@ __device__ __forceinline__ uint32_t activate(const Sched& s, uint32_t tile, uint
         atomicMin(&s_krange[0], kb);
         atomicMax(&s_krange[1], kb);
     }
-    uint32_t const old = atom_or_release(&s.flags[tile], kActive | bits);
+    uint32_t const old = atom_or_release(&s.flags[tile], kActive | bits | pbit);
     if (!(old & kActive)) {
         uint32_t const pos = atomicAdd(&s.ctl->count[nxt], 1u);
         if (pos < s.num_tiles) {

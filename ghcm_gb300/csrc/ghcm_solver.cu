@@ -64,11 +64,11 @@ constexpr int kWideCtas = 8;
 
 // List entries per thread the top-n select keeps in registers between its
 // passes (ids and bins; a list of up to 256 x this many is read once): 7 in
-// the 64-register systolic builds (8 spills), 6 in the block-FIM ones, 4 in
-// the 32-register wide builds.
-template <bool FIM, int CTAS>
+// the 64-register systolic builds of tiles of 16 (8 spills), 6 in the other
+// 64-register builds, 4 in the 32-register wide builds.
+template <int B, bool FIM, int CTAS>
 __host__ __device__ constexpr int select_regs() {
-    return CTAS > 4 ? 4 : (FIM ? 6 : 7);
+    return CTAS > 4 ? 4 : ((FIM || B == 32) ? 6 : 7);
 }
 
 template <int B, bool FIM, int CTAS = max_ctas_per_sm<B>()>
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, CTAS) k_solve(const __gr
     bool ranked = false;
     for (;;) {
         GHCM_PROF_BEGIN(t_bar);
-        bool const ok = wave_barrier<G::THREADS, select_regs<FIM, CTAS>()>(s, s_hist, s_sel, s_state, s_krange);
+        bool const ok = wave_barrier<G::THREADS, select_regs<B, FIM, CTAS>()>(s, s_hist, s_sel, s_state, s_krange);
         GHCM_PROF_END(ctl, 0, t_bar);
         if (!ok) break;
         if (!ranked) {  // the first barrier follows every CTA's sm_enter
@@ -136,8 +136,9 @@ __global__ void __launch_bounds__(TileGeom<B>::THREADS, CTAS) k_solve(const __gr
                     if (tid == 0) atomicOr(&ctl->error, kErrInternal);
                     break;
                 }
-                int const r = solve_tile<B, FIM, (CTAS <= 4)>(s, job, cur ^ 1u, sm, &s_bar, parity, tma_pending, s_word, s_red,
-                                                 s_krange, wave, s_state[kStResid] + 1u);
+                int const r = solve_tile<B, FIM, (CTAS <= 4)>(s, job, cur ^ 1u, sm, &s_bar, parity, tma_pending, s_word,
+                                                              s_red, s_krange, wave, s_state[kStResid] + 1u,
+                                                              act_phase_bit(s_state[kStGen]));
                 if (r == kJobFailed) break;
                 solves += (r == kJobSolved) ? 1u : 0u;
             }
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(WarpTileGeom<B>::THREADS, 3) k_solve_warp(cons
                     break;
                 }
                 int const r = solve_tile_warp<B>(s, job, cur ^ 1u, sm, parity, tma_pending, s_krange, wave,
-                                                 s_state[kStResid] + 1u);
+                                                 s_state[kStResid] + 1u, act_phase_bit(s_state[kStGen]));
                 if (r == kJobFailed) break;
                 solves += (r == kJobSolved) ? 1u : 0u;
             }
@@ -298,7 +299,7 @@ __global__ void k_init_seeds(Sched s, int block) {
             if (px < 0 || py < 0 || px >= static_cast<int>(I.w) || py >= static_cast<int>(I.h)) continue;
             uint32_t const tile = I.tile_base + static_cast<uint32_t>(py / block) * I.tiles_x + px / block;
             s.tmin[tile] = 0.f;
-            activate(s, tile, 0u, 0.f, 0u, nullptr);  // key range of list 0: {0, 0} from the zeroed Ctl
+            activate(s, tile, 0u, 0.f, 0u, nullptr, 0u);  // key range of list 0: {0, 0} from the zeroed Ctl
         }
     }
 }

@@ -80,7 +80,7 @@ enum : int { kJobFailed = 0, kJobSolved = 1, kJobDeferred = 2 };
 template <int B, bool FIM, bool NORMAL = true>
 __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<B>& sm, uint64_t* bar,
                            uint32_t& parity, bool& tma_pending, uint32_t* s_word, float* s_red, uint32_t* s_krange,
-                           uint32_t wave, uint32_t epoch) {
+                           uint32_t wave, uint32_t epoch, uint32_t pbit) {
     using G = TileGeom<B>;
     int const tid = threadIdx.x;
     uint32_t const ii = inst_of(s, tile);
@@ -92,34 +92,44 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
     uint64_t const p_t0 = (tid == 0) ? global_ns() : 0ull;
 #endif
     // Claim: clear the tile's activation state (a later activation re-queues
-    // it), then stage the tile with its halo.
+    // it), and stage the tile with its halo.
     if (tid == 0) {
-        // Both atomics in flight at once. The key is reset first: an activation
-        // landing between the two leaves a lower key on an idle tile (it is
-        // only a priority), while its data is staged, since the flag clear
-        // acquires it.
-        uint32_t const kold = atomicExch(&s.key[tile], inf_bits());
-        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
-        uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
-        s_word[0] = f;
-        s_word[1] = 0u;  // abort flag
-        s_word[4] = 0u;  // edge rows changed by this solve
-        s_word[5] = kold;
-#pragma unroll
-        for (int e = 0; e < 4; ++e) sm.queued[e] = kNone;
-        s_word[6] = kmx;
         // checked builds: the tile lies in its instance and the box starts on a
         // 16-byte boundary; otherwise nothing is staged and the job fails
         bool const tile_ok = GHCM_CHECK(s.ctl, ii < s.num_insts && tc.sx > 0 && tc.sy > 0, 1u);
         bool const x_ok = GHCM_CHECK(s.ctl, ((tc.ox - 4) & 3) == 0, 2u);
-        s_word[3] = (tile_ok && x_ok) ? 0u : 1u;  // 1: nothing staged (written only here)
-        if (tile_ok && x_ok && use_tma) {
+        bool const tma_go = tile_ok && x_ok && use_tma;
+        // The TMA stage goes out before the claim, so that the two round trips
+        // overlap. What the tile and its halo held before this phase is
+        // visible already: the wave barrier acquired it. Newer data comes only
+        // from a neighbour solved in this phase, and a neighbour that changed
+        // the halo activates the tile with this phase's bit (pbit) after its
+        // stores; if the claim finds that bit, it has acquired those stores and
+        // the time box is loaded again below. A neighbour that activates the
+        // tile after the claim re-queues it, as before.
+        if (tma_go) {
             fence_proxy_async();
             mbar_arrive_expect_tx(bar, static_cast<uint32_t>(2 * G::BOX * sizeof(float)));
             tma_load_2d(sm.time, time_map(s, ii), bar, tc.ox - 4, tc.oy - 2);
             tma_load_2d(sm.cost, in_map(s, ii), bar, tc.ox - 4, tc.oy - 2);
             tma_pending = true;
         }
+        // Both atomics in flight at once. The key is reset first: an activation
+        // landing between the two leaves a lower key on an idle tile (it is
+        // only a priority), while its data is staged, since the flag clear
+        // acquires it.
+        uint32_t const kold = atomicExch(&s.key[tile], inf_bits());
+        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask | kActPhaseMask));
+        uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
+        s_word[0] = f;
+        s_word[1] = 0u;  // abort flag
+        s_word[2] = (tma_go && (f & pbit)) ? 1u : 0u;  // load the time box again after the claim
+        s_word[4] = 0u;  // edge rows changed by this solve
+        s_word[5] = kold;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) sm.queued[e] = kNone;
+        s_word[6] = kmx;
+        s_word[3] = (tile_ok && x_ok) ? 0u : 1u;  // 1: nothing staged (written only here)
     }
     __syncthreads();
     uint32_t const flags = s_word[0];
@@ -149,6 +159,26 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         if (tid == 0) learn_defer(s, tile, flags, s_word[5], s_word[6], nxt, s_krange);
         __syncthreads();
         return kJobDeferred;
+    }
+    if (s_word[2]) {
+        // a neighbour solved in this phase activated the tile before the claim:
+        // its stores, acquired by the claim, may postdate the box loaded above
+        __syncthreads();  // every thread has passed the wait above
+        if (!s_word[1]) {
+            if (tid == 0) {
+                fence_proxy_async();
+                mbar_arrive_expect_tx(bar, static_cast<uint32_t>(G::BOX * sizeof(float)));
+                tma_load_2d(sm.time, time_map(s, ii), bar, tc.ox - 4, tc.oy - 2);
+                tma_pending = true;
+            }
+            if (!mbar_wait(bar, parity, s.timeout_ns)) {
+                atomicOr(&s.ctl->error, kErrTimeout);
+                s_word[1] = 1u;
+            } else if (tid == 0) {
+                tma_pending = false;
+            }
+            parity ^= 1u;
+        }
     }
     // fill / fix up the two rings: outside the field is +inf; speed -> cost
     for (int r = tid; r < G::RING; r += G::THREADS) {
@@ -449,12 +479,13 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         if (tile_changed) s.epoch[tile] = epoch;  // the next residual pass re-checks it and its neighbours
         if (solve_count(flags) < s.refresh && (capped || !(s_word[4] & 16u))) atomicAdd(&s.flags[tile], kSolveOne);
         learn_commit(s, tile, useful, wave, sweeps, sm.feat);
-        if (capped) activate(s, tile, kFull, m, nxt, s_krange);
+        if (capped) activate(s, tile, kFull, m, nxt, s_krange, 0u);
     }
     uint32_t const edge_changed = s_word[4];
     if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u) &&
         GHCM_CHECK(s.ctl, nb >= 0 && static_cast<uint32_t>(nb) < s.num_tiles, 7u)) {
-        uint32_t const pos = activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt, s_krange);
+        uint32_t const pos =
+            activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt, s_krange, pbit);
         if (pos != kNoPos) {  // appended now: score it (a re-activation keeps its entry's score)
             sm.queued[e] = static_cast<uint32_t>(nb);
             sm.queued_pos[e] = pos;
@@ -533,7 +564,7 @@ __device__ void residual_warp(const Sched& s, uint32_t nxt, uint32_t warp_global
         if (__any_sync(0xffffffffu, bad)) {
 #pragma unroll
             for (int o = 16; o >= 1; o >>= 1) kmin = fminf(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
-            if (lane == 0) activate(s, tile, kFull, kmin, nxt, s_krange);
+            if (lane == 0) activate(s, tile, kFull, kmin, nxt, s_krange, 0u);
         }
     }
 }

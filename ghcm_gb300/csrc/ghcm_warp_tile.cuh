@@ -42,7 +42,8 @@ struct alignas(128) WarpTileSmem {
 // timed out).
 template <int B>
 __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, WarpTileSmem<B>& sm, uint32_t& parity,
-                                bool& tma_pending, uint32_t* s_krange, uint32_t wave, uint32_t epoch) {
+                                bool& tma_pending, uint32_t* s_krange, uint32_t wave, uint32_t epoch,
+                                uint32_t pbit) {
     using G = TileGeom<B>;
     using W = WarpTileGeom<B>;
     constexpr unsigned FULL = 0xffffffffu;
@@ -58,7 +59,7 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
     // Claim and stage.
     if (lane == 0) {
         uint32_t const kold = atomicExch(&s.key[tile], inf_bits());  // both in flight, as in solve_tile
-        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask));
+        uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask | kActPhaseMask));
         uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
         sm.claim[0] = f;
         sm.claim[1] = kold;
@@ -255,8 +256,8 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
         for (int e = 0; e < 4; ++e)
             if (((imp_mask & ec) >> e) & 1u)
                 activate(s, static_cast<uint32_t>(neighbour_tile(I, tc.tx, tc.ty, e)), kEdgeBit0 << ((e + 2) & 3),
-                         keys[e], nxt, s_krange);
-        if (capped) activate(s, tile, kFull, lmin, nxt, s_krange);
+                         keys[e], nxt, s_krange, pbit);
+        if (capped) activate(s, tile, kFull, lmin, nxt, s_krange, 0u);
 #ifdef GHCM_PROFILE
         atomicAdd(&s.ctl->prof[3], static_cast<unsigned long long>(sweeps));
         atomicMax(&s.ctl->wave_max_sweeps, sweeps);
