@@ -116,8 +116,8 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         }
         // Both atomics in flight at once. The key is reset first: an activation
         // landing between the two leaves a lower key on an idle tile (it is
-        // only a priority), while its data is staged, since the flag clear
-        // acquires it.
+        // only a priority), while its data reaches this solve: the flag clear
+        // acquires it, and its phase bit has the time box loaded again.
         uint32_t const kold = atomicExch(&s.key[tile], inf_bits());
         uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask | kActPhaseMask));
         uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
