@@ -146,51 +146,81 @@ __device__ void tile_speed_stats(const Sched& s, uint32_t tile) {
     }
 }
 
-// Score policy: the model logit of `tile` (tile (tx, ty) of instance I),
-// just appended at entry `pos` of list[nxt] by the calling CTA's solve,
-// computed by the calling warp and kept in that entry's score for the next
-// decision. Every load is issued at once (one round trip; the neighbours'
-// ids come from the coordinates, not from memory). Tiles re-queued in full
-// need no score (they are always taken).
-__device__ void score_queued_warp(const Sched& s, const Inst& I, uint32_t tile, uint32_t tx, uint32_t ty,
-                                  uint32_t nxt, uint32_t pos, uint32_t wave) {
-    const Learn& L = s.learn;
-    uint32_t const flags = __ldcg(&s.flags[tile]);
-    float const key = __uint_as_float(__ldcg(&s.key[tile]));
-    float const kmax = __uint_as_float(__ldcg(&L.kmax[tile]));
-    float const tm = __ldcg(&s.tmin[tile]);
-    uint32_t const ns = __ldcg(&L.nsolve[tile]);
-    float4 const st = __ldg(&L.tstat[tile]);
-    uint32_t const lc = __ldcg(&L.last_change[tile]);
-    float const front = __ldcg(&s.ctl->wave_front);
-    float const span = __ldcg(&s.ctl->wave_span);
-    uint32_t nf[4];
+// Score policy. The state of a tile the calling CTA's solve activates, as
+// the scorer needs it: its flags, keys, smallest time, solves, speed
+// statistics, wave of its last useful solve, its neighbours' flags and the
+// wave's key range. load() is run by the activating thread right after its
+// flag atomic, into the shared-memory slot the scoring warp reads: every
+// load is issued before the first store, so the round trip overlaps the
+// activation's own, and the thread's own key, kmax and flag updates precede
+// the loads in program order and are seen.
+struct QueuedState {
+    float4 st;
+    uint32_t flags, key, kmax, ns, lc, act;
+    float tm, front, span;
+    __device__ __forceinline__ void load(const Sched& s, const Inst& I, uint32_t tile, uint32_t tx, uint32_t ty) {
+        const Learn& L = s.learn;
+        uint32_t const f = __ldcg(&s.flags[tile]);
+        uint32_t const k = __ldcg(&s.key[tile]);
+        uint32_t const km = __ldcg(&L.kmax[tile]);
+        float const t = __ldcg(&s.tmin[tile]);
+        uint32_t const n = __ldcg(&L.nsolve[tile]);
+        float4 const sv = __ldg(&L.tstat[tile]);
+        uint32_t const l = __ldcg(&L.last_change[tile]);
+        float const fr = __ldcg(&s.ctl->wave_front);
+        float const sp = __ldcg(&s.ctl->wave_span);
+        uint32_t nf[4];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        int const nb = neighbour_tile(I, tx, ty, e);
-        nf[e] = nb >= 0 ? __ldcg(&s.flags[nb]) : 0u;
+        for (int e = 0; e < 4; ++e) {
+            int const nb = neighbour_tile(I, tx, ty, e);
+            nf[e] = nb >= 0 ? __ldcg(&s.flags[nb]) : 0u;
+        }
+        uint32_t a = 0u;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) a += (nf[e] & kActive) ? 1u : 0u;
+        flags = f;
+        key = k;
+        kmax = km;
+        tm = t;
+        ns = n;
+        st = sv;
+        lc = l;
+        front = fr;
+        span = sp;
+        act = a;
     }
-    if (flags & kFull) return;
-    int act = 0;
-#pragma unroll
-    for (int e = 0; e < 4; ++e) act += (nf[e] & kActive) ? 1 : 0;
+};
+
+// The model logit of a tile just appended at entry `pos` of list[nxt] by the
+// calling CTA's solve, from its loaded state, computed by the calling warp
+// and kept in that entry's score for the next decision. Tiles re-queued in
+// full need no score (they are always taken).
+__device__ void score_queued_warp(const Sched& s, const QueuedState& q, uint32_t nxt, uint32_t pos, uint32_t wave) {
+    if (q.flags & kFull) return;
     float x[kFeatures];
-    features_from(key, kmax, flags, tm, ns, st, lc, act, wave, front, span, x);
+    features_from(__uint_as_float(q.key), __uint_as_float(q.kmax), q.flags, q.tm, q.ns, q.st, q.lc,
+                  static_cast<int>(q.act), wave, q.front, q.span, x);
     float const z = mlp_logit_warp(g_mlp_params, x);
-    if ((threadIdx.x & 31) == 0) __stcg(&L.lscore[nxt][pos], z);
+    if ((threadIdx.x & 31) == 0) __stcg(&s.learn.lscore[nxt][pos], z);
 }
 
 }  // namespace ghcm
 
 namespace ghcm {
 
-// Claim-time bookkeeping of a block-solve, by one thread: resets the tile's
-// largest activation key and, when tracing, writes the features the
-// scheduler saw into feat. flags / key_bits: the tile's state as claimed.
+// Claim-time bookkeeping of a block-solve, by one thread, in two parts.
+// learn_claim_kmax resets the tile's largest activation key and returns it;
+// it is issued with the claim's other atomics, before the flag clear acquires
+// (an activation landing in between leaves its key for the tile's next
+// queueing: it is only a feature). learn_claim then, when tracing, writes the
+// features the scheduler saw into feat. flags / key_bits / kmx: the tile's
+// state as claimed.
+__device__ __forceinline__ uint32_t learn_claim_kmax(const Sched& s, uint32_t tile) {
+    return s.learn.tstat ? atomicExch(&s.learn.kmax[tile], 0u) : 0u;
+}
 __device__ __forceinline__ uint32_t learn_claim(const Sched& s, uint32_t tile, uint32_t flags, uint32_t key_bits,
-                                                uint32_t wave, float* feat) {
+                                                uint32_t kmx, uint32_t wave, float* feat) {
     if (!s.learn.tstat) return 0u;
-    uint32_t const kmx = atomicExch(&s.learn.kmax[tile], 0u);
     if (s.learn.trace) {
         float f[kFeatures];
         tile_features(s, tile, flags, __uint_as_float(key_bits), __uint_as_float(kmx), wave,

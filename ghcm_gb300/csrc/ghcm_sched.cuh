@@ -77,9 +77,15 @@ constexpr uint32_t kNoPos = 0xffffffffu;
 // src/eikonal_hcm.cpp:451-462. s_krange (the calling CTA's {min, max} key
 // bits of what it activated this phase) is widened to `key`. Returns the
 // tile's position in list[nxt] when this call appended it (it was idle),
-// else kNoPos.
+// else kNoPos. `after_flag` runs right after the flag atomic is issued: loads
+// it makes are in flight with that atomic and the append (a release orders
+// only what comes before it).
+struct NoHook {
+    __device__ void operator()() const {}
+};
+template <class Hook = NoHook>
 __device__ __forceinline__ uint32_t activate(const Sched& s, uint32_t tile, uint32_t bits, float key, uint32_t nxt,
-                                             uint32_t* s_krange, uint32_t pbit) {
+                                             uint32_t* s_krange, uint32_t pbit, Hook after_flag = Hook{}) {
     uint32_t const kb = __float_as_uint(key);
     atomicMin(&s.key[tile], kb);
     if (s.learn.kmax) atomicMax(&s.learn.kmax[tile], kb);
@@ -88,6 +94,7 @@ __device__ __forceinline__ uint32_t activate(const Sched& s, uint32_t tile, uint
         atomicMax(&s_krange[1], kb);
     }
     uint32_t const old = atom_or_release(&s.flags[tile], kActive | bits | pbit);
+    after_flag();
     if (!(old & kActive)) {
         uint32_t const pos = atomicAdd(&s.ctl->count[nxt], 1u);
         if (pos < s.num_tiles) {

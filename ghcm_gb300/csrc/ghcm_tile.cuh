@@ -57,6 +57,7 @@ struct alignas(128) TileSmem {
     float feat[kFeatures]; // trace recorder: features of the current solve
     uint32_t queued[4];    // learned score policy: neighbour queued across edge e, or kNone
     uint32_t queued_pos[4];  // and its entry in the next active list
+    QueuedState queued_state[4];  // and its state for the scorer
 };
 
 constexpr uint32_t kNone = 0xffffffffu;
@@ -118,9 +119,10 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         // landing between the two leaves a lower key on an idle tile (it is
         // only a priority), while its data reaches this solve: the flag clear
         // acquires it, and its phase bit has the time box loaded again.
+        uint32_t const kmx0 = learn_claim_kmax(s, tile);
         uint32_t const kold = atomicExch(&s.key[tile], inf_bits());
         uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask | kActPhaseMask));
-        uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
+        uint32_t const kmx = learn_claim(s, tile, f, kold, kmx0, wave, sm.feat);
         s_word[0] = f;
         s_word[1] = 0u;  // abort flag
         s_word[2] = (tma_go && (f & pbit)) ? 1u : 0u;  // load the time box again after the claim
@@ -482,21 +484,24 @@ __device__ int solve_tile(const Sched& s, uint32_t tile, uint32_t nxt, TileSmem<
         if (capped) activate(s, tile, kFull, m, nxt, s_krange, 0u);
     }
     uint32_t const edge_changed = s_word[4];
+    bool const scoring = s.learn.params && !s.learn.veto;  // learned score policy
     if (tid < 4 * B && ei == 0 && e_imp && ((edge_changed >> e) & 1u) &&
         GHCM_CHECK(s.ctl, nb >= 0 && static_cast<uint32_t>(nb) < s.num_tiles, 7u)) {
         uint32_t const pos =
-            activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt, s_krange, pbit);
+            activate(s, static_cast<uint32_t>(nb), kEdgeBit0 << ((e + 2) & 3), e_key, nxt, s_krange, pbit, [&]() {
+                if (scoring)
+                    sm.queued_state[e].load(s, I, static_cast<uint32_t>(nb), tc.tx + (e == 2) - (e == 0),
+                                            tc.ty + (e == 3) - (e == 1));
+            });
         if (pos != kNoPos) {  // appended now: score it (a re-activation keeps its entry's score)
             sm.queued[e] = static_cast<uint32_t>(nb);
             sm.queued_pos[e] = pos;
         }
     }
-    if (s.learn.params && !s.learn.veto) {  // score policy: score what this solve queued, a warp per tile
+    if (scoring) {  // score what this solve queued, a warp per tile
         __syncthreads();
         for (int q = tid >> 5; q < 4; q += G::THREADS / 32)
-            if (sm.queued[q] != kNone)
-                score_queued_warp(s, I, sm.queued[q], tc.tx + (q == 2) - (q == 0), tc.ty + (q == 3) - (q == 1), nxt,
-                                  sm.queued_pos[q], wave + 1u);
+            if (sm.queued[q] != kNone) score_queued_warp(s, sm.queued_state[q], nxt, sm.queued_pos[q], wave + 1u);
     }
 #ifdef GHCM_PROFILE
     if (tid == 0) {

@@ -58,9 +58,10 @@ __device__ int solve_tile_warp(const Sched& s, uint32_t tile, uint32_t nxt, Warp
 
     // Claim and stage.
     if (lane == 0) {
-        uint32_t const kold = atomicExch(&s.key[tile], inf_bits());  // both in flight, as in solve_tile
+        uint32_t const kmx0 = learn_claim_kmax(s, tile);
+        uint32_t const kold = atomicExch(&s.key[tile], inf_bits());  // all in flight, as in solve_tile
         uint32_t const f = atom_and_acquire(&s.flags[tile], ~(kActive | kFull | kEdgeMask | kActPhaseMask));
-        uint32_t const kmx = learn_claim(s, tile, f, kold, wave, sm.feat);
+        uint32_t const kmx = learn_claim(s, tile, f, kold, kmx0, wave, sm.feat);
         sm.claim[0] = f;
         sm.claim[1] = kold;
         sm.claim[2] = kmx;
