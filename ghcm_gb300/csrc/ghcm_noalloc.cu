@@ -19,8 +19,9 @@
 // wrong results; serialise them. Everything a solve needs zeroed (the control
 // block) or initialised (the per-tile state) is set at the start of each call.
 // The first call on a device looks the array's device address up with
-// cudaGetSymbolAddress (with that device current); make that first call
-// before capturing any stream into a graph.
+// cudaGetSymbolAddress (with that device current). Every call reads the
+// control block back and synchronises its stream, so none can be captured
+// into a CUDA graph.
 #include "ghcm_device.cuh"
 #include "ghcm_host.h"
 

@@ -329,12 +329,12 @@ int ghcm_abi_version(void);
  * static device array of about 7 MiB that every GPU loading the library holds
  * until exit; fields whose tiling exceeds GHCM_NOALLOC_MAX_TILES are rejected
  * with GHCM_ERR_TOO_LARGE. Runs on the current device (cfg->device must be -1
- * or that device) on `stream` and returns when the solve has finished.
- * All calls share the one scratch array: calls that overlap on the GPU (other
- * streams or host threads) race and must be serialised by the caller. The
- * first call on a device looks up the array's device address; make it before
- * capturing a stream into a CUDA graph. No statistics are returned. Plain
- * schedule only (cfg->schedule must be GHCM_SCHEDULE_PLAIN). */
+ * or that device) on `stream` and returns when the solve has finished: it
+ * reads the solve's status back and synchronises `stream`, so it cannot be
+ * captured into a CUDA graph. All calls share the one scratch array: calls
+ * that overlap on the GPU (other streams or host threads) race and must be
+ * serialised by the caller. No statistics are returned. Plain schedule only
+ * (cfg->schedule must be GHCM_SCHEDULE_PLAIN). */
 int ghcm_solve_device_noalloc(const ghcm_config* cfg, const float* d_field, int input_is_speed, uint32_t width,
                               uint32_t height, float h, const uint32_t* d_seeds_xy, uint32_t n_seeds,
                               float* d_time_out, void* stream);
